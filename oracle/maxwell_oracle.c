@@ -20,6 +20,7 @@
 #include <omp.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
 
 typedef om_cplx cx;
 
@@ -1062,7 +1063,7 @@ combine(long len, int ns, cx **in, int m, const cx *coef, int ldc, cx **out)
 }
 
 typedef struct {
-  cx **e, **p, **x, **u;   /* m vectors each */
+  cx **e, **p, **x, **u, **w;   /* m vectors each */
   double *mu, *res;
   int have_p;
 } block_t;
@@ -1116,16 +1117,29 @@ pinvit_step(ctx_t *c, block_t *B)
   return info;
 }
 
+static double
+lobpcg_drop(void)
+{
+  const char *e = getenv("OM_DROP");
+  return e ? atof(e) : 1e-10;
+}
+
+/* Soft locking (Knyazev, SIAM J. Sci. Comput. 23 (2001), BLOPEX): a column
+ * whose residual is at or below the tolerance keeps its Ritz vector in the
+ * basis but contributes no X or P column, so noise-level corrections of
+ * converged pairs cannot spoil the small problem. */
 static int
 lobpcg_step(ctx_t *c, block_t *B)
 {
   const om_opts *o = c->o;
   om_mg *h = c->h;
-  int m = o->m, ns = B->have_p ? 3 * m : 2 * m, i, r;
+  int m = o->m, ns = B->have_p ? 3 * m : 2 * m, i, j, r, na = 0, nr;
   cx **s = malloc(sizeof(cx *) * ns);
   cx *ga = malloc(sizeof(cx) * ns * ns), *gm = malloc(sizeof(cx) * ns * ns);
-  cx *coef = malloc(sizeof(cx) * ns * m);
+  cx *coef = calloc((size_t) ns * m, sizeof(cx));
+  int *idx = malloc(sizeof(int) * ns);
   double *theta = malloc(sizeof(double) * m);
+  cx *sa, *sm, *sc;
   for(i = 0; i < m; i++) {
     precondition(c, B->e[i], B->mu[i], B->x[i]);
     if(o->center && is_gamma(h->xf, h->yf))
@@ -1139,19 +1153,40 @@ lobpcg_step(ctx_t *c, block_t *B)
       s[2 * m + i] = B->p[i];
   }
   gram(c, ns, s, ga, gm);
-  r = om_rr_svqb(ns, ga, gm, m, 1e-10, coef, theta);
+  /* reduced basis: all of E, X and P of the unlocked columns */
+  for(i = 0; i < m; i++)
+    idx[na++] = i;
+  for(j = 1; j < ns / m; j++)
+    for(i = 0; i < m; i++)
+      if(B->res[i] > o->tol)
+        idx[na++] = j * m + i;
+  sa = malloc(sizeof(cx) * na * na); sm = malloc(sizeof(cx) * na * na);
+  sc = malloc(sizeof(cx) * na * m);
+  for(j = 0; j < na; j++)
+    for(i = 0; i < na; i++) {
+      sa[i + (size_t) j * na] = ga[idx[i] + (size_t) idx[j] * ns];
+      sm[i + (size_t) j * na] = gm[idx[i] + (size_t) idx[j] * ns];
+    }
+  nr = om_rr_svqb(na, sa, sm, m, lobpcg_drop(), sc, theta);
+  r = nr;
   if(r < 0) {
-    free(s); free(ga); free(gm); free(coef); free(theta);
+    free(s); free(ga); free(gm); free(coef); free(theta); free(idx);
+    free(sa); free(sm); free(sc);
     return 1;
   }
-  /* P = [X P] C[m:, :], E = S C */
+  for(j = 0; j < m; j++)
+    for(i = 0; i < na; i++)
+      coef[idx[i] + (size_t) j * ns] = sc[i + (size_t) j * na];
+  /* P = [X P] C[m:, :] into u, E = S C into w, then rotate the buffers */
   combine(c->len, ns - m, s + m, m, coef + m, ns, B->u);
+  combine(c->len, ns, s, m, coef, ns, B->w);
   for(i = 0; i < m; i++) {
-    cx *t = B->p[i]; B->p[i] = B->u[i]; B->u[i] = t;
-  }
-  combine(c->len, ns, s, m, coef, ns, B->u);
-  for(i = 0; i < m; i++) {
-    cx *t = B->e[i]; B->e[i] = B->u[i]; B->u[i] = t;
+    cx *t = B->p[i];
+    B->p[i] = B->u[i];
+    B->u[i] = t;
+    t = B->e[i];
+    B->e[i] = B->w[i];
+    B->w[i] = t;
     B->mu[i] = theta[i];
   }
   B->have_p = 1;
@@ -1163,7 +1198,8 @@ lobpcg_step(ctx_t *c, block_t *B)
     }
     B->res[i] = residual(c, B->e[i], B->mu[i]);
   }
-  free(s); free(ga); free(gm); free(coef); free(theta);
+  free(s); free(ga); free(gm); free(coef); free(theta); free(idx);
+  free(sa); free(sm); free(sc);
   return 0;
 }
 
@@ -1187,6 +1223,13 @@ iterate(ctx_t *c, block_t *B, int maxsteps)
     int info = c->o->method ? lobpcg_step(c, B) : pinvit_step(c, B);
     if(info)
       return -(k + 1);
+    if(getenv("OM_DEBUG")) {
+      int i;
+      fprintf(stderr, "l=%d step %d:", c->l, k);
+      for(i = 0; i < c->o->m; i++)
+        fprintf(stderr, " %.1e", B->res[i]);
+      fprintf(stderr, "\n");
+    }
   }
   return k;
 }
@@ -1301,7 +1344,7 @@ om_bloch_solve(const om_opts *o, const double *kappa_fine, int nk,
   c.t1 = calloc(len, sizeof(cx)); c.t2 = calloc(len, sizeof(cx));
   c.tn = calloc(len / 2, sizeof(cx));
   B.e = alloc_block(m, len); B.p = alloc_block(m, len);
-  B.x = alloc_block(m, len); B.u = alloc_block(m, len);
+  B.x = alloc_block(m, len); B.u = alloc_block(m, len); B.w = alloc_block(m, len);
   B.mu = malloc(sizeof(double) * m); B.res = malloc(sizeof(double) * m);
 
   for(kk = 0; kk < nk && status == 0; kk++) {
@@ -1352,6 +1395,7 @@ om_bloch_solve(const om_opts *o, const double *kappa_fine, int nk,
   free(store);
   free_block(lev, m);
   free_block(B.e, m); free_block(B.p, m); free_block(B.x, m); free_block(B.u, m);
+  free_block(B.w, m);
   free(B.mu); free(B.res);
   free(c.t1); free(c.t2); free(c.tn);
   om_mg_free(h);
