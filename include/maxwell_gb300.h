@@ -1,0 +1,187 @@
+/* libmaxwell_gb300: C ABI of the GB300 (sm_103a) Bloch eigensolver.
+ *
+ * Drop-in for the multigrid-preconditioned block eigensolver of sboerm/Maxwell
+ * on one GPU.  The names mirror the reference's interfaces with a _gpu
+ * suffix; every object lives in device memory and holds a BATCH: K Bloch
+ * parameters (k-points) times m vectors.  K = m = 1 gives the reference's
+ * single-vector semantics.
+ *
+ *   reference (file:line)                      this library
+ *   grid2d.h:7-78   grid2d, new/del/coarsen    grid2d_gpu, new/del/coarsen_grid2d_gpu
+ *   edge2d.h:12-29  edge2d                     edge2d_gpu
+ *   edge2d.h:71-291 vector, operator, GS,      *_edge2d_gpu (same argument meaning;
+ *                   transfer, V-cycle, dense    scalars per vector come back as arrays)
+ *   node2d.h:9-158  node2d + its functions     *_node2d_gpu
+ *   linalg.h:7-31   matrix, potrf, potrsv,     matrix_gpu, potrf_matrix_gpu, ...
+ *                   syev, sygv
+ *   exp_bloch2d.c:556-1053 per-k driver flow   mxg_bloch_solve
+ *   (new)                                      mxg_eps_sensitivity
+ *
+ * Scalar ABI (settings.h:5-17 with FIELD_COMPLEX): real = double,
+ * field = double complex.  Host arrays of vectors use the reference's dense
+ * order per vector (densefrom_edge2d, edge2d.c:6137-6152): the n*n x-edge
+ * coefficients (i + j*n) followed by the n*n y-edge coefficients; batches are
+ * [k][vector][entries].
+ *
+ * Errors: every function returns 0 on success, a negative MXG_E* code for a
+ * usage error, or a positive cudaError_t value (the reference's vector
+ * functions return void and assert; its LAPACK wrappers return info,
+ * linalg.c:54-63,261-317, which potrf/syev/sygv_matrix_gpu return through an
+ * info array).  Calls on one grid are stream-ordered; results written to host
+ * memory are complete when the call returns.
+ *
+ * There is no CPU fallback: without a CUDA device every compute call returns
+ * a cudaError_t value.
+ */
+#ifndef MAXWELL_GB300_H
+#define MAXWELL_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+typedef struct { double re, im; } mxg_field;
+#else
+#include <complex.h>
+typedef double _Complex mxg_field;
+#endif
+
+enum { MXG_C64 = 0, MXG_C128 = 1, MXG_CDD = 2 };   /* storage of a vector batch */
+
+#define MXG_EINVAL (-1)     /* bad argument, shape or precision */
+#define MXG_ENOMEM (-2)     /* device allocation failed */
+#define MXG_ECONV (-3)      /* Ritz step broke down (rank-deficient basis) */
+
+typedef struct grid2d_gpu grid2d_gpu;
+typedef struct edge2d_gpu edge2d_gpu;
+typedef struct node2d_gpu node2d_gpu;
+typedef struct matrix_gpu matrix_gpu;
+
+/* ---------- grid2d (grid2d.h:36-78) ---------- */
+/* new_grid2d (grid2d.c:12-32): nx = ny intervals of the unit square, K Bloch
+ * parameters (all factors 1, kappa = 1/eps = 1) */
+grid2d_gpu *new_grid2d_gpu(int nx, int ny, double hx, double hy, int K);
+void del_grid2d_gpu(grid2d_gpu *gr);
+/* coarsen_grid2d (grid2d.c:42-68): kappa averaged over 2x2 children, same factors */
+grid2d_gpu *coarsen_grid2d_gpu(const grid2d_gpu *fine);
+/* gr->eps (the reciprocal permittivity per cell, grid2d.c:191-214), n*n host doubles */
+int setkappa_grid2d_gpu(grid2d_gpu *gr, const double *kappa);
+/* gr->xfactor / gr->yfactor for each of the K Bloch parameters */
+int setbloch_grid2d_gpu(grid2d_gpu *gr, const mxg_field *xfactor, const mxg_field *yfactor);
+int getsize_grid2d_gpu(const grid2d_gpu *gr, int *nx, int *K);
+
+/* ---------- edge2d (edge2d.h:71-291) ---------- */
+edge2d_gpu *new_edge2d_gpu(const grid2d_gpu *gr, int m, int prec);
+void del_edge2d_gpu(edge2d_gpu *x);
+size_t getdimension_edge2d_gpu(const edge2d_gpu *x);          /* 2 nx ny per vector */
+int zero_edge2d_gpu(edge2d_gpu *x);
+int copy_edge2d_gpu(const edge2d_gpu *x, edge2d_gpu *y);      /* converts precision */
+int add_edge2d_gpu(mxg_field alpha, const edge2d_gpu *x, edge2d_gpu *y);
+/* norms and products per (k, vector): out has K*m entries */
+int norm2_edge2d_gpu(const edge2d_gpu *x, double *out);
+int center_edge2d_gpu(edge2d_gpu *x);
+/* y += alpha A x + beta M x (edge2d.c:1335-1650) */
+int addeval_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *x, edge2d_gpu *y);
+/* the same with one beta per (k, vector): the PINVIT defect with its own shift */
+int addeval_shifted_edge2d_gpu(double alpha, const double *beta_per_vector,
+                               const edge2d_gpu *x, edge2d_gpu *y);
+/* x^H (alpha A + beta M) y and x^H M y per (k, vector) (edge2d.c:1652-2027) */
+int energyprod_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *x,
+                          const edge2d_gpu *y, mxg_field *out);
+int massprod_edge2d_gpu(const edge2d_gpu *x, const edge2d_gpu *y, mxg_field *out);
+/* AFW Gauss-Seidel (edge2d.c:2656-3042) */
+int gsforward_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+int gsbackward_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+int gssymm_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+/* transfers (edge2d.c:5583-5705) */
+int prolongation_edge2d_gpu(mxg_field alpha, const edge2d_gpu *c, edge2d_gpu *f);
+int restriction_edge2d_gpu(mxg_field alpha, const edge2d_gpu *f, edge2d_gpu *c);
+/* vcycle_edge2d (edge2d.c:5707-5754): b, x, d arrays of L+1 levels */
+int vcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2d_gpu **x,
+                      edge2d_gpu **d);
+/* densematrix_edge2d (edge2d.c:5870-6116) for every k of the grid */
+int densematrix_edge2d_gpu(mxg_field alpha, mxg_field beta, const grid2d_gpu *gr, matrix_gpu *a);
+/* host <-> device in the reference's dense order (denseto/densefrom_edge2d) */
+int denseto_edge2d_gpu(const mxg_field *host, edge2d_gpu *y);
+int densefrom_edge2d_gpu(const edge2d_gpu *x, mxg_field *host);
+
+/* ---------- node2d (node2d.h:28-158) ---------- */
+node2d_gpu *new_node2d_gpu(const grid2d_gpu *gr, int m, int prec);
+void del_node2d_gpu(node2d_gpu *x);
+int zero_node2d_gpu(node2d_gpu *x);
+int addeval_node2d_gpu(mxg_field alpha, const node2d_gpu *x, node2d_gpu *y);
+int gsforward_node2d_gpu(mxg_field alpha, const node2d_gpu *b, node2d_gpu *x);
+int gsbackward_node2d_gpu(mxg_field alpha, const node2d_gpu *b, node2d_gpu *x);
+int gssymm_node2d_gpu(mxg_field alpha, const node2d_gpu *b, node2d_gpu *x);
+int prolongation_node2d_gpu(mxg_field alpha, const node2d_gpu *c, node2d_gpu *f);
+int restriction_node2d_gpu(mxg_field alpha, const node2d_gpu *f, node2d_gpu *c);
+int gradient_node2d_gpu(mxg_field alpha, const node2d_gpu *x, edge2d_gpu *y);
+int adjgradient_node2d_gpu(mxg_field alpha, const edge2d_gpu *x, node2d_gpu *y);
+int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2d_gpu **x,
+                      node2d_gpu **d);
+int densematrix_node2d_gpu(int fixnull, const grid2d_gpu *gr, matrix_gpu *a);
+int denseto_node2d_gpu(const mxg_field *host, node2d_gpu *y);
+int densefrom_node2d_gpu(const node2d_gpu *x, mxg_field *host);
+
+/* ---------- linalg (linalg.h:7-31): one square matrix per k ---------- */
+matrix_gpu *new_matrix_gpu(int rows, int K);
+void del_matrix_gpu(matrix_gpu *a);
+int upload_matrix_gpu(matrix_gpu *a, const mxg_field *host);      /* K column-major */
+int download_matrix_gpu(const matrix_gpu *a, mxg_field *host);
+/* potrf_matrix (linalg.c:54-63) prepares the coarse solve: the factor is kept
+ * as the explicit inverse, so potrsv applies one matrix-vector product;
+ * info[k] as zpotrf's */
+int potrf_matrix_gpu(matrix_gpu *a, int *info);
+/* sygv_matrix (linalg.c:285-317), itype 1: a <- B-orthonormal eigenvectors,
+ * lambda (K*rows) ascending, info per k */
+int sygv_matrix_gpu(matrix_gpu *a, matrix_gpu *b, double *lambda, int *info);
+/* syev_matrix (linalg.c:254-283) */
+int syev_matrix_gpu(matrix_gpu *a, double *lambda, int *info);
+
+/* ---------- the per-k eigensolver (exp_bloch2d.c:556-1053) ---------- */
+typedef struct {
+  int n0, L;             /* coarse intervals, refinement levels (n = n0 << L) */
+  int ieigs, m;          /* wanted pairs, block size */
+  int method;            /* 0 block PINVIT + Ritz (exp_bloch2d), 1 LOBPCG */
+  int precision;         /* 0 plain FP64, 1 mixed (FP32 multigrid, float-float eigenvectors) */
+  int max_nested;        /* block steps per level of the nested iteration */
+  int max_steps;         /* block steps at the finest level */
+  int prec_steps;        /* edge V-cycles per preconditioner application */
+  int gradient_steps;    /* node V-cycles per gradient lifting */
+  int smoother_steps;    /* nu */
+  int lift_e;            /* LOBPCG: lift the new eigenvector block as well */
+  int center;            /* remove the constant fields at k = 0 */
+  int wave;              /* k-points per batch; batch w starts from batch w-1 */
+  int relative;          /* stopping rule: 0 absolute defect, 1 relative residual */
+  double tol;
+} mxg_solve_opts;
+
+typedef struct mxg_solver mxg_solver;
+/* kappa_fine: n*n host doubles */
+mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine);
+void mxg_solver_free(mxg_solver *s);
+/* Solve nk k-points (factors e^{i kx}, e^{i ky}); outputs lambda = mu - 1
+ * (nk*m), block steps per k (nk), final residual per vector (nk*m) */
+int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xfactor, const mxg_field *yfactor,
+                    double *lambda, int *steps, double *residual);
+/* eigenvectors of the last solved batch: wave k-points x m vectors in dense order */
+int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
+/* device time of the last mxg_bloch_solve in milliseconds, and the number of
+ * kernel launches it issued */
+int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches);
+
+/* ---------- eigenvalue sensitivity (no counterpart in the reference) ---------- */
+/* grad[c] = sum_{k,v} w[k*m+v] d lambda_{k,v} / d eps_c for M-normalised
+ * eigenvectors e (host, nk*m*2n^2 in dense order):
+ * d lambda / d eps_c = -kappa_c^2 |curl_c e|^2 / (hx hy) */
+int mxg_eps_sensitivity(int n, const double *kappa, int nk, const mxg_field *xfactor,
+                        const mxg_field *yfactor, int m, const mxg_field *evec,
+                        const double *weights, double *grad);
+
+int mxg_device_ok(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

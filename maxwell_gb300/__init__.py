@@ -1,0 +1,292 @@
+"""Python access to libmaxwell_gb300 (the C ABI in include/maxwell_gb300.h).
+
+The library is the product; this module only binds it with ctypes for the
+tests, the benchmark and Python callers.  It never computes anything itself
+and has no fallback: if the shared library is missing, importing ``lib()``
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmaxwell_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "maxwell_gb300.h")
+
+C64, C128, CDD = 0, 1, 2
+
+_lib = None
+
+
+class Field(C.Structure):
+    """double complex by value (same registers as a two-double struct on
+    x86-64 and AArch64)."""
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+def fz(z) -> Field:
+    z = complex(z)
+    return Field(z.real, z.imag)
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [(n, C.c_int) for n in (
+        "n0", "L", "ieigs", "m", "method", "precision", "max_nested", "max_steps", "prec_steps",
+        "gradient_steps", "smoother_steps", "lift_e", "center", "wave", "relative")] + [("tol", C.c_double)]
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m maxwell_gb300.build` "
+                              "(or __graft_entry__.build()) first")
+        L = C.CDLL(LIB_PATH)
+        P, I, D, S = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+        protos = {
+            "new_grid2d_gpu": (P, [I, I, D, D, I]),
+            "del_grid2d_gpu": (None, [P]),
+            "coarsen_grid2d_gpu": (P, [P]),
+            "setkappa_grid2d_gpu": (I, [P, P]),
+            "setbloch_grid2d_gpu": (I, [P, P, P]),
+            "new_edge2d_gpu": (P, [P, I, I]),
+            "del_edge2d_gpu": (None, [P]),
+            "new_node2d_gpu": (P, [P, I, I]),
+            "del_node2d_gpu": (None, [P]),
+            "zero_edge2d_gpu": (I, [P]),
+            "copy_edge2d_gpu": (I, [P, P]),
+            "add_edge2d_gpu": (I, [Field, P, P]),
+            "norm2_edge2d_gpu": (I, [P, P]),
+            "center_edge2d_gpu": (I, [P]),
+            "addeval_edge2d_gpu": (I, [Field, Field, P, P]),
+            "addeval_shifted_edge2d_gpu": (I, [D, P, P, P]),
+            "energyprod_edge2d_gpu": (I, [Field, Field, P, P, P]),
+            "massprod_edge2d_gpu": (I, [P, P, P]),
+            "gsforward_edge2d_gpu": (I, [Field, Field, P, P]),
+            "gsbackward_edge2d_gpu": (I, [Field, Field, P, P]),
+            "gssymm_edge2d_gpu": (I, [Field, Field, P, P]),
+            "prolongation_edge2d_gpu": (I, [Field, P, P]),
+            "restriction_edge2d_gpu": (I, [Field, P, P]),
+            "vcycle_edge2d_gpu": (I, [I, I, P, P, P, P]),
+            "densematrix_edge2d_gpu": (I, [Field, Field, P, P]),
+            "denseto_edge2d_gpu": (I, [P, P]),
+            "densefrom_edge2d_gpu": (I, [P, P]),
+            "zero_node2d_gpu": (I, [P]),
+            "addeval_node2d_gpu": (I, [Field, P, P]),
+            "gsforward_node2d_gpu": (I, [Field, P, P]),
+            "gsbackward_node2d_gpu": (I, [Field, P, P]),
+            "gssymm_node2d_gpu": (I, [Field, P, P]),
+            "prolongation_node2d_gpu": (I, [Field, P, P]),
+            "restriction_node2d_gpu": (I, [Field, P, P]),
+            "gradient_node2d_gpu": (I, [Field, P, P]),
+            "adjgradient_node2d_gpu": (I, [Field, P, P]),
+            "vcycle_node2d_gpu": (I, [I, I, P, P, P, P]),
+            "densematrix_node2d_gpu": (I, [I, P, P]),
+            "denseto_node2d_gpu": (I, [P, P]),
+            "densefrom_node2d_gpu": (I, [P, P]),
+            "new_matrix_gpu": (P, [I, I]),
+            "del_matrix_gpu": (None, [P]),
+            "upload_matrix_gpu": (I, [P, P]),
+            "download_matrix_gpu": (I, [P, P]),
+            "potrf_matrix_gpu": (I, [P, P]),
+            "sygv_matrix_gpu": (I, [P, P, P, P]),
+            "syev_matrix_gpu": (I, [P, P, P]),
+            "mxg_solver_new": (P, [P, P]),
+            "mxg_solver_free": (None, [P]),
+            "mxg_bloch_solve": (I, [P, I, P, P, P, P, P]),
+            "mxg_solver_eigenvectors": (I, [P, P]),
+            "mxg_solver_stats": (I, [P, P, P]),
+            "mxg_eps_sensitivity": (I, [I, P, I, P, P, I, P, P, P]),
+            "mxg_device_ok": (I, []),
+        }
+        for name, (res, args) in protos.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def check(code: int, what: str = "call") -> None:
+    if code != 0:
+        raise RuntimeError(f"libmaxwell_gb300 {what} failed with status {code}")
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/maxwell_gb300.h."""
+    import re
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt)
+    skip = {"if", "sizeof", "return"}
+    out = []
+    for n in names:
+        if n in skip or n.isupper():
+            continue
+        if n not in out:
+            out.append(n)
+    return out
+
+
+# ----------------------------------------------------------------------
+# thin object wrappers used by the tests
+# ----------------------------------------------------------------------
+class Grid:
+    def __init__(self, n: int, K: int = 1, kappa=None, factors=None, _handle=None):
+        self.n, self.K = n, K
+        self.h = _handle if _handle is not None else lib().new_grid2d_gpu(n, n, 1.0 / n, 1.0 / n, K)
+        if not self.h:
+            raise RuntimeError("new_grid2d_gpu failed")
+        if kappa is not None:
+            check(lib().setkappa_grid2d_gpu(self.h, _ptr(np.ascontiguousarray(kappa, np.float64))), "setkappa")
+        if factors is not None:
+            self.set_bloch(factors)
+
+    def set_bloch(self, factors):
+        f = np.asarray(factors, np.complex128).reshape(self.K, 2)
+        xf, yf = np.ascontiguousarray(f[:, 0]), np.ascontiguousarray(f[:, 1])
+        check(lib().setbloch_grid2d_gpu(self.h, _ptr(xf), _ptr(yf)), "setbloch")
+
+    def coarsen(self) -> "Grid":
+        h = lib().coarsen_grid2d_gpu(self.h)
+        return Grid(self.n // 2, self.K, _handle=h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.del_grid2d_gpu(self.h)
+
+
+class Edge:
+    def __init__(self, g: Grid, m: int = 1, prec: int = C128, data=None):
+        self.g, self.m, self.prec = g, m, prec
+        self.h = lib().new_edge2d_gpu(g.h, m, prec)
+        if not self.h:
+            raise RuntimeError("new_edge2d_gpu failed")
+        if data is not None:
+            self.put(data)
+
+    @property
+    def shape(self):
+        return (self.g.K, self.m, 2 * self.g.n * self.g.n)
+
+    def put(self, data):
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(data, np.complex128), self.shape))
+        check(lib().denseto_edge2d_gpu(_ptr(a), self.h), "denseto_edge2d")
+
+    def get(self) -> np.ndarray:
+        a = np.zeros(self.shape, np.complex128)
+        check(lib().densefrom_edge2d_gpu(self.h, _ptr(a)), "densefrom_edge2d")
+        return a
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.del_edge2d_gpu(self.h)
+
+
+class Node:
+    def __init__(self, g: Grid, m: int = 1, prec: int = C128, data=None):
+        self.g, self.m, self.prec = g, m, prec
+        self.h = lib().new_node2d_gpu(g.h, m, prec)
+        if not self.h:
+            raise RuntimeError("new_node2d_gpu failed")
+        if data is not None:
+            self.put(data)
+
+    @property
+    def shape(self):
+        return (self.g.K, self.m, self.g.n * self.g.n)
+
+    def put(self, data):
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(data, np.complex128), self.shape))
+        check(lib().denseto_node2d_gpu(_ptr(a), self.h), "denseto_node2d")
+
+    def get(self) -> np.ndarray:
+        a = np.zeros(self.shape, np.complex128)
+        check(lib().densefrom_node2d_gpu(self.h, _ptr(a)), "densefrom_node2d")
+        return a
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.del_node2d_gpu(self.h)
+
+
+class Matrix:
+    def __init__(self, rows: int, K: int = 1):
+        self.rows, self.K = rows, K
+        self.h = lib().new_matrix_gpu(rows, K)
+        if not self.h:
+            raise RuntimeError("new_matrix_gpu failed")
+
+    def get(self) -> np.ndarray:
+        a = np.zeros((self.K, self.rows, self.rows), np.complex128)
+        check(lib().download_matrix_gpu(self.h, _ptr(a)), "download_matrix")
+        return np.transpose(a, (0, 2, 1))   # column-major per k
+
+    def put(self, a):
+        a = np.ascontiguousarray(np.transpose(np.asarray(a, np.complex128).reshape(self.K, self.rows, self.rows), (0, 2, 1)))
+        check(lib().upload_matrix_gpu(self.h, _ptr(a)), "upload_matrix")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.del_matrix_gpu(self.h)
+
+
+class Solver:
+    """The batched per-k eigensolver (mxg_bloch_solve)."""
+
+    def __init__(self, kappa_fine, *, n0, L, ieigs, m, method=1, precision=1, max_nested=20,
+                 max_steps=60, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1, center=1,
+                 wave=1, relative=1, tol=1e-8):
+        self.o = SolveOpts(n0, L, ieigs, m, method, precision, max_nested, max_steps, prec_steps,
+                           gradient_steps, smoother_steps, lift_e, center, wave, relative, tol)
+        self.n = n0 << L
+        self.m, self.wave = m, wave
+        k = np.ascontiguousarray(kappa_fine, np.float64)
+        self.h = lib().mxg_solver_new(C.byref(self.o), _ptr(k))
+        if not self.h:
+            raise RuntimeError("mxg_solver_new failed (bad options or out of device memory)")
+
+    def solve(self, factors):
+        f = np.asarray(factors, np.complex128).reshape(-1, 2)
+        nk = f.shape[0]
+        xf, yf = np.ascontiguousarray(f[:, 0]), np.ascontiguousarray(f[:, 1])
+        lam = np.zeros((nk, self.m))
+        steps = np.zeros(nk, np.int32)
+        res = np.zeros((nk, self.m))
+        check(lib().mxg_bloch_solve(self.h, nk, _ptr(xf), _ptr(yf), _ptr(lam), _ptr(steps), _ptr(res)),
+              "mxg_bloch_solve")
+        return lam, steps, res
+
+    def eigenvectors(self) -> np.ndarray:
+        a = np.zeros((self.wave, self.m, 2 * self.n * self.n), np.complex128)
+        check(lib().mxg_solver_eigenvectors(self.h, _ptr(a)), "eigenvectors")
+        return a
+
+    def stats(self):
+        ms, launches = C.c_double(0), C.c_long(0)
+        lib().mxg_solver_stats(self.h, C.byref(ms), C.byref(launches))
+        return ms.value, launches.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.mxg_solver_free(self.h)
+
+
+def eps_sensitivity(n, kappa, factors, vecs, weights):
+    f = np.asarray(factors, np.complex128).reshape(-1, 2)
+    nk = f.shape[0]
+    vecs = np.ascontiguousarray(vecs, np.complex128)
+    m = vecs.shape[1]
+    w = np.ascontiguousarray(weights, np.float64).reshape(nk * m)
+    g = np.zeros(n * n)
+    xf, yf = np.ascontiguousarray(f[:, 0]), np.ascontiguousarray(f[:, 1])
+    check(lib().mxg_eps_sensitivity(n, _ptr(np.ascontiguousarray(kappa, np.float64)), nk, _ptr(xf), _ptr(yf),
+                                    m, _ptr(vecs), _ptr(w), _ptr(g)), "mxg_eps_sensitivity")
+    return g

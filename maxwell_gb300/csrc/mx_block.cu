@@ -1,0 +1,505 @@
+// Eigenvector-block kernels of the Ritz step (exp_bloch2d.c:956-1053,
+// test_lobpcg2d.c:217-365) batched over k-points:
+//   residual / Rayleigh statistics  (defects of exp_bloch2d.c:1012-1018)
+//   Gram matrices S^H (A+M) S, S^H M S   (energyprod/massprod, edge2d.c:1652-2027)
+//   block linear combination E = S C     (the add_edge2d loops, exp_bloch2d.c:1006-1010)
+//   permittivity sensitivity of eigenvalues
+//
+// Precision: the eigenvector block E is stored as float-float (cdd) in the
+// mixed solver and as c128 in the plain FP64 solver; the search blocks X, P
+// are c64 (mixed) or c128 (plain).  Everything that decides eigenvalue
+// accuracy (the residual, e^H (A+M) e, e^H M e and the E-E Gram block) is
+// computed in float-float or FP64; the Gram entries that involve X or P only
+// steer the subspace and are computed in FP32 in the mixed solver.
+//
+// The Gram uses the cell form of the operator: S^H A S = sum over cells of
+// axy*kappa_c * curl_c(S)^H curl_c(S), which avoids the cancellation of
+// forming A S first, plus the edge form of the mass matrix.
+#include "mx_common.cuh"
+#include "mx_internal.h"
+
+using namespace mx;
+
+namespace {
+
+template <typename R>
+__device__ __forceinline__ Seam<R> seam_of(const double* ph, int k, int n) {
+  Seam<R> s;
+  s.xf = cfrom<R>(ph[4 * k + 0], ph[4 * k + 1]);
+  s.yf = cfrom<R>(ph[4 * k + 2], ph[4 * k + 3]);
+  s.n = n;
+  return s;
+}
+
+template <typename S, typename R>
+struct EA {
+  const S* base;
+  int n, m;
+  Seam<R> seam;
+  __device__ __forceinline__ cx<R> operator()(int p, int i, int j) const {
+    cx<R> ph;
+    bool w = seam.wrap(i, j, ph);
+    cx<R> v = Store<S, R>::ld(base + ((size_t) (p * n + j) * n + i) * m);
+    return w ? ph * v : v;
+  }
+};
+
+template <typename R> __device__ __forceinline__ R rf(double d) { return Real<R>::from(d); }
+
+template <typename R> struct KapB;
+template <> struct KapB<float> {
+  const float* p; int n;
+  __device__ float operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
+};
+template <> struct KapB<double> {
+  const double* p; int n;
+  __device__ double operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
+};
+template <> struct KapB<dd> {
+  const float* p; int n;
+  __device__ dd operator()(int i, int j) const {
+    float2 v = reinterpret_cast<const float2*>(p)[wrapi(i, n) + wrapi(j, n) * n];
+    return dd_make(v.x, v.y);
+  }
+};
+template <typename R> KapB<R> kapb(mxk_kappa k, int n);
+template <> KapB<float> kapb<float>(mxk_kappa k, int n) { KapB<float> r; r.p = k.f; r.n = n; return r; }
+template <> KapB<double> kapb<double>(mxk_kappa k, int n) { KapB<double> r; r.p = k.d; r.n = n; return r; }
+template <> KapB<dd> kapb<dd>(mxk_kappa k, int n) { KapB<dd> r; r.p = k.dd; r.n = n; return r; }
+
+template <typename R, typename A>
+__device__ __forceinline__ cx<R> curlc(const A& E, int i, int j) {
+  return E(0, i, j) - E(0, i, j + 1) - E(1, i, j) + E(1, i + 1, j);
+}
+
+// ------------------------------------------------------------------
+// residual and Rayleigh statistics
+// ------------------------------------------------------------------
+constexpr int NSTAT = 5;
+
+template <typename SE, typename SR, typename R>
+__global__ void k_block_residual(int n, int m, int K, const double* __restrict__ ph, KapB<R> kap,
+                                 const double* __restrict__ mu, const SE* __restrict__ e,
+                                 SR* __restrict__ rout, double* __restrict__ stats) {
+  // block: m lanes (v) x rows; grid (G, K)
+  int k = blockIdx.y;
+  int v = threadIdx.x % m, row = threadIdx.x / m, rows = blockDim.x / m;
+  Lay L{n, m, K};
+  EA<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, seam_of<R>(ph, k, n)};
+  R axy = rf<R>((double) n * (double) n), mm = rf<R>(1.0 / 6.0);
+  R muv = rf<R>(mu[(size_t) k * m + v]);
+  R four = rf<R>(4.0);
+  R s_r2 = Real<R>::zero(), s_v2 = Real<R>::zero(), s_ew = Real<R>::zero(), s_ev = Real<R>::zero(),
+    s_ewi = Real<R>::zero();
+  size_t nsite = (size_t) n * n;
+  if (row < rows) {
+    for (size_t site = (size_t) blockIdx.x * rows + row; site < nsite; site += (size_t) gridDim.x * rows) {
+      int i = (int) (site % n), j = (int) (site / n);
+      cx<R> cc = curlc<R>(E, i, j);
+      cx<R> cb = curlc<R>(E, i, j - 1);
+      cx<R> cl = curlc<R>(E, i - 1, j);
+      cx<R> x0 = E(0, i, j), y0 = E(1, i, j);
+      cx<R> vx = scal(mm, scal(four, x0) + E(0, i, j + 1) + E(0, i, j - 1));
+      cx<R> vy = scal(mm, scal(four, y0) + E(1, i + 1, j) + E(1, i - 1, j));
+      cx<R> wx = scal(axy, scal(kap(i, j), cc) - scal(kap(i, j - 1), cb)) + vx;
+      cx<R> wy = scal(axy, scal(kap(i - 1, j), cl) - scal(kap(i, j), cc)) + vy;
+      cx<R> rx = wx - scal(muv, vx), ry = wy - scal(muv, vy);
+      if (rout) {
+        Store<SR, R>::st(rout + L.edge(k, 0, j, i, v), rx);
+        Store<SR, R>::st(rout + L.edge(k, 1, j, i, v), ry);
+      }
+      s_r2 += rx.re * rx.re + rx.im * rx.im + ry.re * ry.re + ry.im * ry.im;
+      s_v2 += vx.re * vx.re + vx.im * vx.im + vy.re * vy.re + vy.im * vy.im;
+      s_ew += x0.re * wx.re + x0.im * wx.im + y0.re * wy.re + y0.im * wy.im;
+      s_ev += x0.re * vx.re + x0.im * vx.im + y0.re * vy.re + y0.im * vy.im;
+      s_ewi += x0.re * wx.im - x0.im * wx.re + y0.re * wy.im - y0.im * wy.re;
+    }
+  }
+  __shared__ double sh[NSTAT][256];
+  sh[0][threadIdx.x] = Real<R>::to_double(s_r2);
+  sh[1][threadIdx.x] = Real<R>::to_double(s_v2);
+  sh[2][threadIdx.x] = Real<R>::to_double(s_ew);
+  sh[3][threadIdx.x] = Real<R>::to_double(s_ev);
+  sh[4][threadIdx.x] = Real<R>::to_double(s_ewi);
+  __syncthreads();
+  if (threadIdx.x < m * NSTAT) {
+    int q = threadIdx.x / m, vv = threadIdx.x % m;
+    double t = 0.0;
+    for (int r = 0; r < rows; r++) t += sh[q][r * m + vv];
+    atomicAdd(stats + ((size_t) k * m + vv) * NSTAT + q, t);
+  }
+}
+
+// ------------------------------------------------------------------
+// Gram matrices.  One CTA handles a chunk of sites of one k.  Per tile of
+// TS sites it stages, for every basis column, the cell curl, the x and y
+// edge values and the mass stencil at those edges; then every thread
+// accumulates its share of the lower-triangle entries.  Partial sums per CTA
+// go to scratch and a second kernel adds them in a fixed order.
+// Columns of the first block are "high" (float-float or FP64): entries with
+// both columns high are accumulated in that arithmetic.
+// ------------------------------------------------------------------
+constexpr int GT = 256;   // threads
+constexpr int TS = 16;    // sites per tile
+
+struct GramArgs {
+  int n, m, K, nb, ns;
+  int precs[4];
+  const void* ptrs[4];
+  const double* ph;
+  mxk_kappa kap;
+  int chunks;              // CTAs per k
+  double* partial;         // [K][chunks][nent][4]  (ga re, ga im, gm re, gm im)
+};
+
+__device__ __forceinline__ cx<float> ld_any_f(int prec, const void* base, size_t off) {
+  if (prec == MX_C64) return Store<float2, float>::ld((const float2*) base + off);
+  if (prec == MX_CDD) return Store<cdd, float>::ld((const cdd*) base + off);
+  return Store<double2, float>::ld((const double2*) base + off);
+}
+
+// HI = dd for the mixed solver (column block 0 is cdd, the other blocks c64),
+// double for the plain solver (every block c128, every column high).
+template <typename HI>
+__global__ void k_block_gram(GramArgs a, int mh) {
+  int k = blockIdx.y, chunk = blockIdx.x;
+  int n = a.n, m = a.m, ns = a.ns;
+  int nent = ns * (ns + 1) / 2;
+  Lay L{n, m, a.K};
+  extern __shared__ double smd[];
+  // staging per site and column: curl, x, y, (Mx), (My)
+  cx<HI>* hi = reinterpret_cast<cx<HI>*>(smd);                        // TS*mh*5
+  cx<float>* lo = reinterpret_cast<cx<float>*>(hi + TS * mh * 5);      // TS*ns*5
+  HI* kap_h = reinterpret_cast<HI*>(lo + TS * ns * 5);                // TS
+  float* kap_t = reinterpret_cast<float*>(kap_h + TS);                // TS
+  Seam<float> sf = seam_of<float>(a.ph, k, n);
+  Seam<HI> sh = seam_of<HI>(a.ph, k, n);
+  constexpr int MAXE = 5;   // ns <= 48 -> nent <= 1176 <= 5*256
+  cx<float> acc_a[MAXE], acc_m[MAXE];
+  cx<HI> hacc_a[MAXE], hacc_m[MAXE];
+  int ei[MAXE], ej[MAXE];
+  for (int t = 0; t < MAXE; t++) {
+    acc_a[t] = czero<float>(); acc_m[t] = czero<float>();
+    hacc_a[t] = czero<HI>(); hacc_m[t] = czero<HI>();
+    int e = threadIdx.x + t * GT;
+    ei[t] = -1; ej[t] = -1;
+    if (e < nent) {
+      // row-major lower triangle: e = i(i+1)/2 + j, j <= i
+      int i = (int) ((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+      while (i * (i + 1) / 2 > e) i--;
+      while ((i + 1) * (i + 2) / 2 <= e) i++;
+      ei[t] = i; ej[t] = e - i * (i + 1) / 2;
+    }
+  }
+  HI mmh = Real<HI>::from(1.0 / 6.0), fourh = Real<HI>::from(4.0);
+  float mmf = 1.0f / 6.0f;
+  size_t nsite = (size_t) n * n;
+  size_t per = (nsite + a.chunks - 1) / a.chunks;
+  size_t s0 = (size_t) chunk * per, s1 = s0 + per < nsite ? s0 + per : nsite;
+  for (size_t base = s0; base < s1; base += TS) {
+    __syncthreads();
+    for (int w = threadIdx.x; w < TS * ns; w += GT) {
+      int ts = w / ns, col = w % ns;
+      size_t site = base + ts;
+      if (site >= s1) continue;
+      int i = (int) (site % n), j = (int) (site / n);
+      int b = col / m, v = col % m;
+      int prec = a.precs[b];
+      size_t o0 = L.edge(k, 0, 0, 0, v);
+      cx<float>* ls = lo + ((size_t) ts * ns + col) * 5;
+      if (col < mh) {
+        cx<HI> c, x0, y0, mxv, myv;
+        if (prec == MX_CDD) {
+          EA<cdd, HI> E{(const cdd*) a.ptrs[b] + o0, n, m, sh};
+          c = curlc<HI>(E, i, j); x0 = E(0, i, j); y0 = E(1, i, j);
+          mxv = scal(mmh, scal(fourh, x0) + E(0, i, j + 1) + E(0, i, j - 1));
+          myv = scal(mmh, scal(fourh, y0) + E(1, i + 1, j) + E(1, i - 1, j));
+        } else {
+          EA<double2, HI> E{(const double2*) a.ptrs[b] + o0, n, m, sh};
+          c = curlc<HI>(E, i, j); x0 = E(0, i, j); y0 = E(1, i, j);
+          mxv = scal(mmh, scal(fourh, x0) + E(0, i, j + 1) + E(0, i, j - 1));
+          myv = scal(mmh, scal(fourh, y0) + E(1, i + 1, j) + E(1, i - 1, j));
+        }
+        cx<HI>* hs = hi + ((size_t) ts * mh + col) * 5;
+        hs[0] = c; hs[1] = x0; hs[2] = y0; hs[3] = mxv; hs[4] = myv;
+        ls[0] = mkc((float) Real<HI>::to_double(c.re), (float) Real<HI>::to_double(c.im));
+        ls[1] = mkc((float) Real<HI>::to_double(x0.re), (float) Real<HI>::to_double(x0.im));
+        ls[2] = mkc((float) Real<HI>::to_double(y0.re), (float) Real<HI>::to_double(y0.im));
+        ls[3] = mkc((float) Real<HI>::to_double(mxv.re), (float) Real<HI>::to_double(mxv.im));
+        ls[4] = mkc((float) Real<HI>::to_double(myv.re), (float) Real<HI>::to_double(myv.im));
+      } else {
+        const void* pb = a.ptrs[b];
+        auto X = [&](int p, int ii, int jj) {
+          cx<float> phz;
+          bool wr = sf.wrap(ii, jj, phz);
+          cx<float> val = ld_any_f(prec, pb, o0 + ((size_t) (p * n + jj) * n + ii) * m);
+          return wr ? phz * val : val;
+        };
+        cx<float> x0 = X(0, i, j), y0 = X(1, i, j);
+        ls[0] = x0 - X(0, i, j + 1) - y0 + X(1, i + 1, j);
+        ls[1] = x0;
+        ls[2] = y0;
+        ls[3] = scal(mmf, scal(4.0f, x0) + X(0, i, j + 1) + X(0, i, j - 1));
+        ls[4] = scal(mmf, scal(4.0f, y0) + X(1, i + 1, j) + X(1, i - 1, j));
+      }
+    }
+    for (int ts = threadIdx.x; ts < TS; ts += GT) {
+      size_t site = base + ts;
+      if (site < s1) {
+        kap_t[ts] = a.kap.f[site];
+        kap_h[ts] = Real<HI>::from(a.kap.d[site]);
+      } else {
+        kap_t[ts] = 0.0f;
+        kap_h[ts] = Real<HI>::zero();
+      }
+    }
+    __syncthreads();
+    int nts = (int) (s1 - base < (size_t) TS ? s1 - base : (size_t) TS);
+    for (int t = 0; t < MAXE; t++) {
+      int i = ei[t], j = ej[t];
+      if (i < 0) continue;
+      if (i < mh && j < mh) {
+        cx<HI> sa = czero<HI>(), sm2 = czero<HI>();
+        for (int ts = 0; ts < nts; ts++) {
+          const cx<HI>* hs = hi + (size_t) ts * mh * 5;
+          sa += scal(kap_h[ts], conjc(hs[i * 5]) * hs[j * 5]);
+          sm2 += conjc(hs[i * 5 + 1]) * hs[j * 5 + 3] + conjc(hs[i * 5 + 2]) * hs[j * 5 + 4];
+        }
+        hacc_a[t] += sa;
+        hacc_m[t] += sm2;
+      } else {
+        cx<float> sa = czero<float>(), sm2 = czero<float>();
+        for (int ts = 0; ts < nts; ts++) {
+          const cx<float>* ls = lo + (size_t) ts * ns * 5;
+          sa += scal(kap_t[ts], conjc(ls[i * 5]) * ls[j * 5]);
+          sm2 += conjc(ls[i * 5 + 1]) * ls[j * 5 + 3] + conjc(ls[i * 5 + 2]) * ls[j * 5 + 4];
+        }
+        acc_a[t] += sa;
+        acc_m[t] += sm2;
+      }
+    }
+  }
+  double axy = (double) n * (double) n;
+  double* out = a.partial + (((size_t) k * a.chunks + chunk) * nent) * 4;
+  for (int t = 0; t < MAXE; t++) {
+    int e = threadIdx.x + t * GT;
+    if (e >= nent) continue;
+    double ar = Real<HI>::to_double(hacc_a[t].re) + (double) acc_a[t].re;
+    double ai = Real<HI>::to_double(hacc_a[t].im) + (double) acc_a[t].im;
+    double mr = Real<HI>::to_double(hacc_m[t].re) + (double) acc_m[t].re;
+    double mi = Real<HI>::to_double(hacc_m[t].im) + (double) acc_m[t].im;
+    // A + M = axy * (sum over cells of kappa conj(curl_i) curl_j) + M
+    out[(size_t) e * 4 + 0] = axy * ar + mr;
+    out[(size_t) e * 4 + 1] = axy * ai + mi;
+    out[(size_t) e * 4 + 2] = mr;
+    out[(size_t) e * 4 + 3] = mi;
+  }
+}
+
+__global__ void k_gram_reduce(int ns, int K, int chunks, const double* __restrict__ partial,
+                              double* __restrict__ ga, double* __restrict__ gm) {
+  int nent = ns * (ns + 1) / 2;
+  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t) nent * K) return;
+  int k = (int) (t / nent), e = (int) (t % nent);
+  int i = (int) ((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+  while (i * (i + 1) / 2 > e) i--;
+  while ((i + 1) * (i + 2) / 2 <= e) i++;
+  int j = e - i * (i + 1) / 2;
+  double s[4] = {0, 0, 0, 0};
+  for (int c = 0; c < chunks; c++) {
+    const double* p = partial + (((size_t) k * chunks + c) * nent + e) * 4;
+    s[0] += p[0]; s[1] += p[1]; s[2] += p[2]; s[3] += p[3];
+  }
+  // entry (i,j) = s_i^H K s_j; lower triangle i >= j, upper by symmetry
+  double* A = ga + (size_t) k * 2 * ns * ns;
+  double* M = gm + (size_t) k * 2 * ns * ns;
+  A[2 * ((size_t) j * ns + i) + 0] = s[0];
+  A[2 * ((size_t) j * ns + i) + 1] = s[1];
+  M[2 * ((size_t) j * ns + i) + 0] = s[2];
+  M[2 * ((size_t) j * ns + i) + 1] = s[3];
+  A[2 * ((size_t) i * ns + j) + 0] = s[0];
+  A[2 * ((size_t) i * ns + j) + 1] = -s[1];
+  M[2 * ((size_t) i * ns + j) + 0] = s[2];
+  M[2 * ((size_t) i * ns + j) + 1] = -s[3];
+}
+
+// ------------------------------------------------------------------
+// block combine: out(k, e, j) = sum_i coef[k](row0 + i, j) S_i(k, e)
+// ------------------------------------------------------------------
+struct CombArgs {
+  int n, m, K, nb, ldc, row0;
+  int precs[4];
+  const void* ptrs[4];
+  const double* coef;
+};
+
+template <typename SO, typename RO>
+__global__ void k_block_combine(CombArgs a, SO* __restrict__ out) {
+  int k = blockIdx.y;
+  int m = a.m;
+  size_t per_k = (size_t) 2 * a.n * a.n * m;
+  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= per_k) return;
+  int j = (int) (t % m);
+  size_t ent = t / m;   // (plane, site)
+  size_t kbase = (size_t) k * per_k;
+  const double* C = a.coef + (size_t) k * 2 * a.ldc * m;
+  cx<RO> acc_hi = czero<RO>();
+  cx<float> acc_lo = czero<float>();
+  for (int b = 0; b < a.nb; b++) {
+    int prec = a.precs[b];
+    for (int i = 0; i < m; i++) {
+      size_t row = (size_t) a.row0 + (size_t) b * m + i;
+      double cr = C[2 * ((size_t) j * a.ldc + row)], ci = C[2 * ((size_t) j * a.ldc + row) + 1];
+      size_t off = kbase + ent * m + i;
+      if (prec == MX_C64) {
+        float2 s = ((const float2*) a.ptrs[b])[off];
+        acc_lo += mkc((float) cr, (float) ci) * mkc(s.x, s.y);
+      } else if (prec == MX_CDD) {
+        cx<RO> s = Store<cdd, RO>::ld((const cdd*) a.ptrs[b] + off);
+        acc_hi += cfrom<RO>(cr, ci) * s;
+      } else {
+        cx<RO> s = Store<double2, RO>::ld((const double2*) a.ptrs[b] + off);
+        acc_hi += cfrom<RO>(cr, ci) * s;
+      }
+    }
+  }
+  cx<RO> res = acc_hi + cfrom<RO>((double) acc_lo.re, (double) acc_lo.im);
+  Store<SO, RO>::st(out + kbase + ent * m + j, res);
+}
+
+// ------------------------------------------------------------------
+// sensitivity: grad[c] = -n^2 kappa_c^2 sum_{k,v} w_kv |curl_c e_kv|^2
+// ------------------------------------------------------------------
+template <typename S, typename R>
+__global__ void k_eps_sensitivity(int n, int m, int K, const double* __restrict__ ph,
+                                  const double* __restrict__ kappa, const double* __restrict__ w,
+                                  const S* __restrict__ e, double* __restrict__ grad) {
+  size_t c = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (size_t) n * n) return;
+  int i = (int) (c % n), j = (int) (c / n);
+  Lay L{n, m, K};
+  double s = 0.0;
+  for (int k = 0; k < K; k++) {
+    Seam<R> sm = seam_of<R>(ph, k, n);
+    for (int v = 0; v < m; v++) {
+      double wv = w[(size_t) k * m + v];
+      if (wv == 0.0) continue;
+      EA<S, R> E{e + L.edge(k, 0, 0, 0, v), n, m, sm};
+      cx<R> cu = curlc<R>(E, i, j);
+      double re = Real<R>::to_double(cu.re), im = Real<R>::to_double(cu.im);
+      s += wv * (re * re + im * im);
+    }
+  }
+  double kc = kappa[c];
+  grad[c] = -(double) n * n * kc * kc * s;
+}
+
+}  // namespace
+
+extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kappa kap, const double* mu,
+                                  int pe, const void* e, int pr, void* rout, double* stats, mx_stream s) {
+  int rows = 256 / m;
+  if (m > 32) return (int) cudaErrorInvalidValue;
+  size_t nsite = (size_t) n * n;
+  unsigned G = (unsigned) ((nsite + (size_t) rows * 8 - 1) / ((size_t) rows * 8));
+  if (G < 1) G = 1;
+  if (G > 4096) G = 4096;
+  dim3 g(G, K), b(256);
+  cudaStream_t st = (cudaStream_t) s;
+  if (pe == MX_CDD && (pr == MX_C64 || !rout))
+    k_block_residual<cdd, float2, dd><<<g, b, 0, st>>>(n, m, K, ph, kapb<dd>(kap, n), mu, (const cdd*) e, (float2*) rout, stats);
+  else if (pe == MX_C128 && (pr == MX_C128 || !rout))
+    k_block_residual<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), mu, (const double2*) e, (double2*) rout, stats);
+  else if (pe == MX_C128 && pr == MX_C64)
+    k_block_residual<double2, float2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), mu, (const double2*) e, (float2*) rout, stats);
+  else if (pe == MX_C64 && (pr == MX_C64 || !rout))
+    k_block_residual<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, kapb<float>(kap, n), mu, (const float2*) e, (float2*) rout, stats);
+  else
+    return (int) cudaErrorInvalidValue;
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+static int gram_chunks(int K, size_t nsite) {
+  int c = (4 * 152 + K - 1) / K;
+  if (c < 8) c = 8;
+  if (c > 256) c = 256;
+  size_t maxc = (nsite + TS - 1) / TS;
+  if ((size_t) c > maxc) c = (int) maxc;
+  return c;
+}
+
+extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa kap, int nb, const int* precs,
+                              const void* const* ptrs, double* ga, double* gm, double* scratch,
+                              size_t scratch_bytes, mx_stream s) {
+  if (nb < 1 || nb > 4 || nb * m > 48) return (int) cudaErrorInvalidValue;
+  GramArgs a;
+  a.n = n; a.m = m; a.K = K; a.nb = nb; a.ns = nb * m;
+  for (int b = 0; b < 4; b++) {
+    a.precs[b] = b < nb ? precs[b] : MX_C64;
+    a.ptrs[b] = b < nb ? ptrs[b] : nullptr;
+  }
+  a.ph = ph; a.kap = kap;
+  int nent = a.ns * (a.ns + 1) / 2;
+  a.chunks = gram_chunks(K, (size_t) n * n);
+  size_t need = (size_t) K * a.chunks * nent * 4 * sizeof(double);
+  while (need > scratch_bytes && a.chunks > 1) {
+    a.chunks /= 2;
+    need = (size_t) K * a.chunks * nent * 4 * sizeof(double);
+  }
+  if (need > scratch_bytes) return (int) cudaErrorMemoryAllocation;
+  a.partial = scratch;
+  cudaStream_t st = (cudaStream_t) s;
+  dim3 g(a.chunks, K);
+  bool all128 = true;
+  for (int b = 0; b < nb; b++) all128 = all128 && precs[b] == MX_C128;
+  bool hi_dd = precs[0] == MX_CDD;
+  int mh = all128 ? a.ns : (precs[0] == MX_C64 ? 0 : m);
+  size_t hsz = hi_dd ? sizeof(cx<dd>) : sizeof(cx<double>);
+  size_t smem = hsz * TS * mh * 5 + sizeof(cx<float>) * TS * a.ns * 5 + (hsz / 2 + sizeof(float)) * TS + 16;
+  if (hi_dd) {
+    cudaFuncSetAttribute(k_block_gram<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_block_gram<dd><<<g, GT, smem, st>>>(a, mh);
+  } else {
+    cudaFuncSetAttribute(k_block_gram<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_block_gram<double><<<g, GT, smem, st>>>(a, mh);
+  }
+  MX_CHECK_LAUNCH();
+  size_t work = (size_t) nent * K;
+  k_gram_reduce<<<(unsigned) ((work + 255) / 256), 256, 0, st>>>(a.ns, K, a.chunks, scratch, ga, gm);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, const void* const* ptrs,
+                                 const double* coef, int ldc, int row0, int pout, void* out, mx_stream s) {
+  if (nb < 1 || nb > 4) return (int) cudaErrorInvalidValue;
+  CombArgs a;
+  a.n = n; a.m = m; a.K = K; a.nb = nb; a.ldc = ldc; a.row0 = row0; a.coef = coef;
+  for (int b = 0; b < 4; b++) {
+    a.precs[b] = b < nb ? precs[b] : MX_C64;
+    a.ptrs[b] = b < nb ? ptrs[b] : nullptr;
+  }
+  size_t per_k = (size_t) 2 * n * n * m;
+  dim3 g((unsigned) ((per_k + 255) / 256), K), b(256);
+  cudaStream_t st = (cudaStream_t) s;
+  if (pout == MX_CDD) k_block_combine<cdd, dd><<<g, b, 0, st>>>(a, (cdd*) out);
+  else if (pout == MX_C128) k_block_combine<double2, double><<<g, b, 0, st>>>(a, (double2*) out);
+  else k_block_combine<float2, float><<<g, b, 0, st>>>(a, (float2*) out);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+extern "C" int mxk_eps_sensitivity(int n, int m, int K, const double* ph, const double* kappa, const double* w,
+                                   int pe, const void* e, double* grad, mx_stream s) {
+  size_t nc = (size_t) n * n;
+  dim3 g((unsigned) ((nc + 255) / 256)), b(256);
+  cudaStream_t st = (cudaStream_t) s;
+  if (pe == MX_CDD) k_eps_sensitivity<cdd, dd><<<g, b, 0, st>>>(n, m, K, ph, kappa, w, (const cdd*) e, grad);
+  else if (pe == MX_C128) k_eps_sensitivity<double2, double><<<g, b, 0, st>>>(n, m, K, ph, kappa, w, (const double2*) e, grad);
+  else k_eps_sensitivity<float2, float><<<g, b, 0, st>>>(n, m, K, ph, kappa, w, (const float2*) e, grad);
+  MX_CHECK_LAUNCH();
+  return 0;
+}

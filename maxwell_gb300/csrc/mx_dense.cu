@@ -1,0 +1,395 @@
+// Batched small dense complex linear algebra in FP64 (one CTA per k-point).
+// These matrices are tiny (coarse grids of 2*8*8 = 128 edges, Ritz systems of
+// at most 3m = 48 columns), so FP64 on GB300 is affordable here; they replace
+// the reference's LAPACK calls (linalg.c:48-317):
+//   mxk_hpd_inverse    zpotrf + ztrsm pairs of the coarse-grid solves
+//   mxk_heev           zheev (cyclic Jacobi with Brent-Luk parallel ordering)
+//   mxk_rayleigh_ritz  zhegv of the Ritz step, as Cholesky-QR of the Gram
+//                      matrix with column dropping followed by Jacobi
+// Matrices are column-major, complex stored as (re, im) double pairs.
+#include "mx_common.cuh"
+#include "mx_internal.h"
+
+#include <math.h>
+
+using namespace mx;
+
+namespace {
+
+constexpr int DT = 256;   // threads per CTA
+
+struct Z {
+  double re, im;
+};
+__device__ __forceinline__ Z zmk(double a, double b) { Z z; z.re = a; z.im = b; return z; }
+__device__ __forceinline__ Z zadd(Z a, Z b) { return zmk(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ Z zsub(Z a, Z b) { return zmk(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ Z zmul(Z a, Z b) { return zmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+__device__ __forceinline__ Z zcmul(Z a, Z b) { return zmk(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re); }  // conj(a) b
+__device__ __forceinline__ Z zconj(Z a) { return zmk(a.re, -a.im); }
+__device__ __forceinline__ Z zscal(double s, Z a) { return zmk(s * a.re, s * a.im); }
+__device__ __forceinline__ double zabs2(Z a) { return a.re * a.re + a.im * a.im; }
+__device__ __forceinline__ Z zdiv(Z a, Z b) {
+  double d = zabs2(b);
+  return zmk((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+}
+
+#define AT(M, ld, i, j) (reinterpret_cast<Z*>(M)[(size_t) (j) * (ld) + (i)])
+
+__device__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sh[0] = t;
+  __syncthreads();
+  t = sh[0];
+  __syncthreads();
+  return t;
+}
+
+// ------------------------------------------------------------------
+// Gauss-Jordan inverse of a Hermitian positive definite matrix (no
+// pivoting is needed for HPD input)
+// ------------------------------------------------------------------
+__global__ void k_hpd_inverse(int N, double* a, int* info) {
+  extern __shared__ double sm[];
+  Z* f = reinterpret_cast<Z*>(sm);
+  Z* rowp = f + N;
+  double* A = a + (size_t) blockIdx.x * 2 * N * N;
+  int bad = 0;
+  for (int p = 0; p < N; p++) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) f[i] = AT(A, N, i, p);
+    __syncthreads();
+    Z piv = f[p];
+    if (!(piv.re > 0.0)) bad = p + 1;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      Z v = j == p ? zmk(1.0, 0.0) : AT(A, N, p, j);
+      rowp[j] = zdiv(v, piv);
+    }
+    __syncthreads();
+    for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+      int i = (int) (e % N), j = (int) (e / N);
+      if (i == p) AT(A, N, i, j) = rowp[j];
+      else {
+        Z v = j == p ? zmk(0.0, 0.0) : AT(A, N, i, j);
+        AT(A, N, i, j) = zsub(v, zmul(f[i], rowp[j]));
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && info) info[blockIdx.x] = bad;
+}
+
+// ------------------------------------------------------------------
+// y_k = Ainv_k x_k on a level-0 block: the block of one k-point is a
+// row-major N x m matrix (dense row r at offset r*m)
+// ------------------------------------------------------------------
+template <typename S, typename R>
+__global__ void k_coarse_apply(int N, int m, const double* __restrict__ ainv, const S* __restrict__ x,
+                               S* __restrict__ y) {
+  int k = blockIdx.y;
+  const Z* Ai = reinterpret_cast<const Z*>(ainv) + (size_t) k * N * N;
+  const S* xk = x + (size_t) k * N * m;
+  S* yk = y + (size_t) k * N * m;
+  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t) N * m) return;
+  int v = (int) (t % m), r = (int) (t / m);
+  cx<R> acc = czero<R>();
+  for (int c = 0; c < N; c++) {
+    Z a = Ai[(size_t) c * N + r];
+    acc += cfrom<R>(a.re, a.im) * Store<S, R>::ld(xk + (size_t) c * m + v);
+  }
+  Store<S, R>::st(yk + (size_t) r * m + v, acc);
+}
+
+// ------------------------------------------------------------------
+// Cyclic Jacobi for a Hermitian N x N matrix in global memory (full storage),
+// eigenvectors accumulated in Zm; Brent-Luk round-robin ordering lets the
+// N/2 rotations of one round run concurrently.  Rotation: for the pair (p,q)
+// with a_pq = g e, g = |a_pq|, tau = (a_qq - a_pp)/(2g),
+// t = sgn(tau)/(|tau| + sqrt(1+tau^2)), c = 1/sqrt(1+t^2), s = t c, and
+// V = [[c, s e], [-s conj(e), c]] on (p,q); A <- V^H A V, Z <- Z V.
+// ------------------------------------------------------------------
+__device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd, int* shi, int max_sweeps) {
+  // shd: 4 * (N/2 + 1) doubles of rotation data, plus 32 for reductions
+  int Np = N + (N & 1);   // pad to even with a dummy index N
+  int half = Np / 2;
+  double* cs = shd;             // c
+  double* sn = shd + half;      // s
+  double* er = shd + 2 * half;  // Re e
+  double* ei = shd + 3 * half;  // Im e
+  double* red = shd + 4 * half;
+  int* pp = shi;
+  int* qq = shi + half;
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+    int i = (int) (e % N), j = (int) (e / N);
+    AT(Zm, N, i, j) = zmk(i == j ? 1.0 : 0.0, 0.0);
+    if (i < j) AT(A, N, i, j) = zconj(AT(A, N, j, i));   // complete from the lower triangle
+    if (i == j) AT(A, N, i, i).im = 0.0;
+  }
+  __syncthreads();
+  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+    double off = 0.0, dia = 0.0;
+    for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+      int i = (int) (e % N), j = (int) (e / N);
+      double v = zabs2(AT(A, N, i, j));
+      if (i == j) dia += v; else off += v;
+    }
+    off = block_sum(off, red);
+    dia = block_sum(dia, red);
+    if (off <= 1e-30 * dia || off == 0.0) break;
+    for (int r = 0; r < Np - 1; r++) {
+      for (int s = threadIdx.x; s < half; s += blockDim.x) {
+        int a = s == 0 ? 0 : 1 + (s - 1 + r) % (Np - 1);
+        int bpos = Np - 1 - s;
+        int b = 1 + (bpos - 1 + r) % (Np - 1);
+        int p = a < b ? a : b, q = a < b ? b : a;
+        double c = 1.0, sv = 0.0, xr = 1.0, xi = 0.0;
+        if (q < N) {
+          Z apq = AT(A, N, p, q);
+          double g = sqrt(zabs2(apq));
+          if (g > 0.0) {
+            double app = AT(A, N, p, p).re, aqq = AT(A, N, q, q).re;
+            double tau = (aqq - app) / (2.0 * g);
+            double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            sv = t * c;
+            xr = apq.re / g;
+            xi = apq.im / g;
+          }
+        }
+        pp[s] = p; qq[s] = q; cs[s] = c; sn[s] = sv; er[s] = xr; ei[s] = xi;
+      }
+      __syncthreads();
+      // columns: A <- A V, Z <- Z V
+      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
+        int s = (int) (e / N), i = (int) (e % N);
+        int p = pp[s], q = qq[s];
+        if (q >= N || sn[s] == 0.0) continue;
+        Z ex = zmk(er[s], ei[s]);
+        double c = cs[s], sv = sn[s];
+        Z ap = AT(A, N, i, p), aq = AT(A, N, i, q);
+        AT(A, N, i, p) = zsub(zscal(c, ap), zscal(sv, zmul(zconj(ex), aq)));
+        AT(A, N, i, q) = zadd(zscal(sv, zmul(ex, ap)), zscal(c, aq));
+        Z zp = AT(Zm, N, i, p), zq = AT(Zm, N, i, q);
+        AT(Zm, N, i, p) = zsub(zscal(c, zp), zscal(sv, zmul(zconj(ex), zq)));
+        AT(Zm, N, i, q) = zadd(zscal(sv, zmul(ex, zp)), zscal(c, zq));
+      }
+      __syncthreads();
+      // rows: A <- V^H A
+      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
+        int s = (int) (e / N), j = (int) (e % N);
+        int p = pp[s], q = qq[s];
+        if (q >= N || sn[s] == 0.0) continue;
+        Z ex = zmk(er[s], ei[s]);
+        double c = cs[s], sv = sn[s];
+        Z ap = AT(A, N, p, j), aq = AT(A, N, q, j);
+        AT(A, N, p, j) = zsub(zscal(c, ap), zscal(sv, zmul(ex, aq)));
+        AT(A, N, q, j) = zadd(zscal(sv, zmul(zconj(ex), ap)), zscal(c, aq));
+      }
+      __syncthreads();
+    }
+  }
+  // eigenvalues, then sort ascending (selection sort by one thread on the
+  // index permutation; N <= 256)
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < N; i++) w[i] = AT(A, N, i, i).re;
+    for (int i = 0; i < N; i++) {
+      int mi = i;
+      for (int j = i + 1; j < N; j++)
+        if (w[j] < w[mi]) mi = j;
+      if (mi != i) {
+        double tw = w[i]; w[i] = w[mi]; w[mi] = tw;
+        for (int r = 0; r < N; r++) {
+          Z tz = AT(Zm, N, r, i);
+          AT(Zm, N, r, i) = AT(Zm, N, r, mi);
+          AT(Zm, N, r, mi) = tz;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
+  extern __shared__ double sm[];
+  int half = (N + 1) / 2 + 1;
+  double* A = a + (size_t) blockIdx.x * 2 * N * N;
+  double* Zm = zwork + (size_t) blockIdx.x * 2 * N * N;
+  jacobi_cta(N, A, Zm, w + (size_t) blockIdx.x * N, sm, reinterpret_cast<int*>(sm + 4 * half + 32), 60);
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x)
+    reinterpret_cast<Z*>(A)[e] = reinterpret_cast<Z*>(Zm)[e];
+  if (threadIdx.x == 0 && info) info[blockIdx.x] = 0;
+}
+
+// ------------------------------------------------------------------
+// Rayleigh-Ritz from Gram matrices (see mx_internal.h)
+// workspace per k: 4 * ns * ns complex doubles
+// ------------------------------------------------------------------
+__global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, const double* __restrict__ gm,
+                                const int* __restrict__ sel, double drop, double* coef, double* theta,
+                                int* info, double* work) {
+  extern __shared__ double sm[];
+  int k = blockIdx.x;
+  int half = (ns + 1) / 2 + 1;
+  double* shd = sm;                                  // jacobi rotation data: 4*half + 32
+  double* d = shd + 4 * half + 32;                   // ns
+  double* wv = d + ns;                               // ns
+  int* shi = reinterpret_cast<int*>(wv + ns);        // 2*half
+  int* idx = shi + 2 * half;                         // ns
+  int* kept = idx + ns;                              // ns
+  int* cnt = kept + ns;                              // 2
+  const double* GA = ga + (size_t) k * 2 * ns * ns;
+  const double* GM = gm + (size_t) k * 2 * ns * ns;
+  double* W0 = work + (size_t) k * 8 * ns * ns;      // scaled Gram, then R
+  double* W1 = W0 + 2 * ns * ns;                     // T = D R^-1
+  double* W2 = W1 + 2 * ns * ns;                     // G_A T, then projected A
+  double* W3 = W2 + 2 * ns * ns;                     // Jacobi eigenvectors
+  if (threadIdx.x == 0) {
+    int na = 0;
+    for (int i = 0; i < ns; i++)
+      if (!sel || sel[(size_t) k * ns + i]) idx[na++] = i;
+    cnt[0] = na;
+  }
+  __syncthreads();
+  int na = cnt[0];
+  for (int i = threadIdx.x; i < na; i += blockDim.x) {
+    double g = reinterpret_cast<const Z*>(GM)[(size_t) idx[i] * ns + idx[i]].re;
+    d[i] = g > 0.0 ? 1.0 / sqrt(g) : 0.0;
+  }
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < (size_t) na * na; e += blockDim.x) {
+    int i = (int) (e % na), j = (int) (e / na);
+    Z g = reinterpret_cast<const Z*>(GM)[(size_t) idx[j] * ns + idx[i]];
+    AT(W0, na, i, j) = zscal(d[i] * d[j], g);
+  }
+  __syncthreads();
+  // right-looking Cholesky with column dropping: W0 -> R (upper), kept flags
+  for (int j = 0; j < na; j++) {
+    double piv = AT(W0, na, j, j).re;
+    bool keep = piv > drop && d[j] > 0.0;
+    double rjj = keep ? sqrt(piv) : 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) kept[j] = keep;
+    for (int l = j + threadIdx.x; l < na; l += blockDim.x) {
+      Z v = AT(W0, na, j, l);
+      AT(W0, na, j, l) = keep ? (l == j ? zmk(rjj, 0.0) : zscal(1.0 / rjj, v)) : zmk(0.0, 0.0);
+    }
+    __syncthreads();
+    if (keep)
+      for (size_t e = threadIdx.x; e < (size_t) (na - j - 1) * (na - j - 1); e += blockDim.x) {
+        int i = j + 1 + (int) (e % (na - j - 1)), l = j + 1 + (int) (e / (na - j - 1));
+        if (i <= l) AT(W0, na, i, l) = zsub(AT(W0, na, i, l), zcmul(AT(W0, na, j, i), AT(W0, na, j, l)));
+      }
+    __syncthreads();
+  }
+  // compact the kept indices
+  if (threadIdx.x == 0) {
+    int r = 0;
+    for (int j = 0; j < na; j++)
+      if (kept[j]) kept[r++] = j;
+    cnt[1] = r;
+  }
+  __syncthreads();
+  int r = cnt[1];
+  if (r < m) {
+    if (threadIdx.x == 0) info[k] = -1 - r;
+    return;
+  }
+  // T (na x r): column c solves R[kept,kept] t = e_c, rows scaled by d
+  for (int c = threadIdx.x; c < r; c += blockDim.x) {
+    for (int i = 0; i < na; i++) AT(W1, na, i, c) = zmk(0.0, 0.0);
+    for (int a = r - 1; a >= 0; a--) {
+      int ia = kept[a];
+      Z s = zmk(a == c ? 1.0 : 0.0, 0.0);
+      for (int b = a + 1; b < r; b++) s = zsub(s, zmul(AT(W0, na, ia, kept[b]), AT(W1, na, kept[b], c)));
+      AT(W1, na, ia, c) = zscal(1.0 / AT(W0, na, ia, ia).re, s);
+    }
+    for (int i = 0; i < na; i++) AT(W1, na, i, c) = zscal(d[i], AT(W1, na, i, c));
+  }
+  __syncthreads();
+  // W3 <- G_A T  (na x r), then W2 <- T^H W3 (r x r)
+  for (size_t e = threadIdx.x; e < (size_t) na * r; e += blockDim.x) {
+    int i = (int) (e % na), c = (int) (e / na);
+    Z s = zmk(0.0, 0.0);
+    for (int l = 0; l < na; l++)
+      s = zadd(s, zmul(reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]], AT(W1, na, l, c)));
+    AT(W3, na, i, c) = s;
+  }
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < (size_t) r * r; e += blockDim.x) {
+    int a = (int) (e % r), c = (int) (e / r);
+    Z s = zmk(0.0, 0.0);
+    for (int l = 0; l < na; l++) s = zadd(s, zcmul(AT(W1, na, l, a), AT(W3, na, l, c)));
+    AT(W2, r, a, c) = s;
+  }
+  __syncthreads();
+  jacobi_cta(r, W2, W3, wv, shd, shi, 60);
+  // coefficients: rows idx[i] <- (T Y)[i, j], other rows zero
+  for (size_t e = threadIdx.x; e < (size_t) ns * m; e += blockDim.x) {
+    int i = (int) (e % ns), j = (int) (e / ns);
+    reinterpret_cast<Z*>(coef)[(size_t) k * ns * m + (size_t) j * ns + i] = zmk(0.0, 0.0);
+  }
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < (size_t) na * m; e += blockDim.x) {
+    int i = (int) (e % na), j = (int) (e / na);
+    Z s = zmk(0.0, 0.0);
+    for (int l = 0; l < r; l++) s = zadd(s, zmul(AT(W1, na, i, l), AT(W3, r, l, j)));
+    reinterpret_cast<Z*>(coef)[(size_t) k * ns * m + (size_t) j * ns + idx[i]] = s;
+  }
+  for (int j = threadIdx.x; j < m; j += blockDim.x) theta[(size_t) k * m + j] = wv[j];
+  if (threadIdx.x == 0) info[k] = r;
+}
+
+size_t jacobi_smem(int N) {
+  int half = (N + 1) / 2 + 1;
+  return sizeof(double) * (4 * half + 32) + sizeof(int) * 2 * half;
+}
+
+}  // namespace
+
+extern "C" int mxk_hpd_inverse(int N, int K, double* a, int* info, mx_stream s) {
+  k_hpd_inverse<<<K, DT, 2 * N * sizeof(Z), (cudaStream_t) s>>>(N, a, info);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+template <typename S, typename R>
+static int L_coarse_apply(int N, int m, int K, const double* ainv, const void* x, void* y, cudaStream_t st) {
+  dim3 g((unsigned) (((size_t) N * m + 127) / 128), K);
+  k_coarse_apply<S, R><<<g, 128, 0, st>>>(N, m, ainv, (const S*) x, (S*) y);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+extern "C" int mxk_coarse_apply(int N, int m, int K, const double* ainv, int prec, const void* x, void* y,
+                                int is_edge, int n, mx_stream s) {
+  (void) is_edge;
+  (void) n;
+  cudaStream_t st = (cudaStream_t) s;
+  if (prec == MX_C64) return L_coarse_apply<float2, float>(N, m, K, ainv, x, y, st);
+  if (prec == MX_C128) return L_coarse_apply<double2, double>(N, m, K, ainv, x, y, st);
+  return L_coarse_apply<cdd, dd>(N, m, K, ainv, x, y, st);
+}
+
+extern "C" int mxk_heev(int N, int K, double* a, double* zwork, double* w, int* info, mx_stream s) {
+  k_heev<<<K, DT, jacobi_smem(N), (cudaStream_t) s>>>(N, a, zwork, w, info);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+extern "C" int mxk_rayleigh_ritz(int ns, int m, int K, const double* ga, const double* gm, const int* sel,
+                                 double drop, double* coef, double* theta, int* info, double* work,
+                                 mx_stream s) {
+  size_t smem = jacobi_smem(ns) + sizeof(int) * (2 * ns + 4) + sizeof(double) * (2 * ns + 2);
+  k_rayleigh_ritz<<<K, DT, smem, (cudaStream_t) s>>>(ns, m, ga, gm, sel, drop, coef, theta, info, work);
+  MX_CHECK_LAUNCH();
+  return 0;
+}

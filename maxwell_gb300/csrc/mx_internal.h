@@ -1,0 +1,132 @@
+/* Internal launch interface of libmaxwell_gb300 (C linkage so that the C
+ * host driver can call it).  Every function enqueues on `stream` and returns
+ * a cudaError_t value (0 on success).  Pointers are device pointers in the
+ * batched layout documented in mx_common.cuh. */
+#ifndef MX_INTERNAL_H
+#define MX_INTERNAL_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *mx_stream;
+
+enum { MX_C64 = 0, MX_C128 = 1, MX_CDD = 2 };
+
+/* sizes of one complex entry */
+size_t mxk_elem_size(int prec);
+
+/* per-level reciprocal permittivity in three precisions */
+typedef struct {
+  const float *f;        /* n*n */
+  const double *d;       /* n*n */
+  const float *dd;       /* 2*n*n: (hi, lo) pairs */
+} mxk_kappa;
+
+/* ---- edge space ---- */
+/* y = cy*y + alpha*A x + beta_kv*M x; beta_kv (K*m doubles) or NULL -> beta */
+int mxk_edge_apply(int n, int m, int K, const double *phases, mxk_kappa kap,
+                   double alpha, double beta, const double *beta_kv, double cy,
+                   int prec_x, const void *x, int prec_y, void *y, mx_stream s);
+/* AFW line Gauss-Seidel sweep in the reference's row order; dir 0 forward,
+ * 1 backward, 2 symmetric (forward then backward) */
+int mxk_edge_gs(int n, int m, int K, const double *phases, mxk_kappa kap,
+                double alpha, double beta, int dir, int prec,
+                const void *b, void *x, mx_stream s);
+int mxk_edge_prolong(int nc, int m, int K, const double *phases, double alpha,
+                     int prec, const void *c, void *f, mx_stream s);
+int mxk_edge_restrict(int nc, int m, int K, const double *phases, double alpha,
+                      int prec, const void *f, void *c, mx_stream s);
+
+/* ---- node space ---- */
+int mxk_node_apply(int n, int m, int K, const double *phases, double alpha, double cy,
+                   int prec, const void *x, void *y, mx_stream s);
+int mxk_node_gs(int n, int m, int K, const double *phases, double alpha, int dir,
+                int prec, const void *b, void *x, mx_stream s);
+int mxk_node_prolong(int nc, int m, int K, const double *phases, double alpha,
+                     int prec, const void *c, void *f, mx_stream s);
+int mxk_node_restrict(int nc, int m, int K, const double *phases, double alpha,
+                      int prec, const void *f, void *c, mx_stream s);
+/* e = ce*e + alpha * G v  (node -> edge) */
+int mxk_gradient(int n, int m, int K, const double *phases, double alpha,
+                 int prec_v, const void *v, int prec_e, void *e, mx_stream s);
+/* v = cv*v + alpha * G^H (mass ? M e : e)  (edge -> node) */
+int mxk_adjgradient(int n, int m, int K, const double *phases, double alpha, int mass,
+                    double cv, int prec_e, const void *e, int prec_v, void *v, mx_stream s);
+
+/* ---- block BLAS-1 (len complex entries) ---- */
+int mxk_zero(int prec, void *x, size_t len, mx_stream s);
+int mxk_convert(int prec_x, const void *x, int prec_y, void *y, size_t len, mx_stream s);
+/* y += a * x with a complex scalar (re, im) */
+int mxk_axpy(double are, double aim, int prec_x, const void *x, int prec_y, void *y,
+             size_t len, mx_stream s);
+/* out[2*(k*m+v)] += sum conj(x) y over `per` entries per vector (out zeroed by the caller) */
+int mxk_dot(size_t per, int m, int K, int prec_x, const void *x, int prec_y, const void *y,
+            double *out, mx_stream s);
+/* Remove the mean of each plane of every (k, vector) (center_edge2d at k = 0);
+ * only applied to k-points whose flag is set. */
+int mxk_center(int n, int m, int K, const int *gamma_flag, int prec, void *x, mx_stream s);
+
+/* ---- coarse dense matrices (one per k, column-major, complex double) ---- */
+/* A = alpha*A + beta*M on the 2n^2 edges of level 0 */
+int mxk_dense_edge(int n, int K, const double *phases, mxk_kappa kap, double alpha,
+                   double beta, double *a, mx_stream s);
+/* Q1 Laplace on n^2 nodes; fixnull adds 0.1/N^2 to every entry at k = 0 */
+int mxk_dense_node(int n, int K, const double *phases, int fixnull, double *a, mx_stream s);
+
+/* ---- batched small dense linear algebra (complex double, one matrix per k) ---- */
+/* in-place inverse of K Hermitian positive definite N x N matrices; info[k] != 0 on breakdown */
+int mxk_hpd_inverse(int N, int K, double *a, int *info, mx_stream s);
+/* y[k] = A[k] x[k] for K blocks, x,y with m columns in the batched layout of a
+ * level-0 edge (N = 2n^2) or node (N = n^2) block */
+int mxk_coarse_apply(int N, int m, int K, const double *ainv, int prec, const void *x,
+                     void *y, int is_edge, int n, mx_stream s);
+/* Hermitian eigendecomposition by parallel cyclic Jacobi: a (lower triangle
+ * used) is overwritten with eigenvectors, w with ascending eigenvalues;
+ * zwork: K*N*N complex doubles of scratch */
+int mxk_heev(int N, int K, double *a, double *zwork, double *w, int *info, mx_stream s);
+/* Rayleigh-Ritz on Gram matrices: reduced basis (sel[k*ns+i] != 0 keeps
+ * column i), unit-diagonal scaling, Cholesky with column dropping
+ * (pivot^2 <= drop), Jacobi on the projected A.  Outputs the lowest m Ritz
+ * values and the ns x m coefficients (zero rows for dropped columns). */
+/* work: 8*ns*ns doubles per k */
+int mxk_rayleigh_ritz(int ns, int m, int K, const double *ga, const double *gm,
+                      const int *sel, double drop, double *coef, double *theta,
+                      int *info, double *work, mx_stream s);
+
+/* ---- block (eigenvector) kernels ---- */
+/* For every (k,v): W = (A+M) e, V = M e (arithmetic of prec_e);
+ * r = W - mu V written to rout (prec_r) when rout != NULL;
+ * stats[(k*m+v)*5 + q] += { |r|^2, |V|^2, Re e^H W, Re e^H V, Im e^H W } */
+int mxk_block_residual(int n, int m, int K, const double *phases, mxk_kappa kap,
+                       const double *mu, int prec_e, const void *e, int prec_r, void *rout,
+                       double *stats, mx_stream s);
+/* Gram matrices of the basis S = [blocks...]: nb blocks of m vectors each,
+ * block b with precision precs[b] at ptrs[b].  ga = S^H (A+M) S, gm = S^H M S,
+ * full ns x ns (ns = nb*m) per k, column-major, complex double. */
+int mxk_block_gram(int n, int m, int K, const double *phases, mxk_kappa kap, int nb,
+                   const int *precs, const void *const *ptrs, double *ga, double *gm,
+                   double *scratch, size_t scratch_bytes, mx_stream s);
+/* out_j = sum_i coef(i,j) S_i for the blocks listed; coef is ns x m per k,
+ * only rows [row0, row0 + nb*m) are used */
+int mxk_block_combine(int n, int m, int K, int nb, const int *precs, const void *const *ptrs,
+                      const double *coef, int ldc, int row0, int prec_out, void *out,
+                      mx_stream s);
+/* per-cell eigenvalue sensitivity: grad[c] = -n^2 kappa_c^2 sum_{k,v} w[k*m+v] |curl_c e|^2 */
+int mxk_eps_sensitivity(int n, int m, int K, const double *phases, const double *kappa,
+                        const double *weights, int prec_e, const void *e, double *grad,
+                        mx_stream s);
+
+/* accessors of the public handles (mx_abi.c) */
+struct grid2d_gpu;
+struct edge2d_gpu;
+const double *mxg__grid_phases(const struct grid2d_gpu *g);
+void *mxg__edge_data(const struct edge2d_gpu *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

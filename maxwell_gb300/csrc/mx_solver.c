@@ -1,0 +1,605 @@
+/* The per-k eigensolver of exp_bloch2d (exp_bloch2d.c:520-1053) for a batch
+ * of k-points solved together on one GPU.
+ *
+ * Flow per batch ("wave") of K k-points:
+ *   - coarse dense generalized eigenproblem on level 0 for every k
+ *     (exp_bloch2d.c:530-554), skipping the zero eigenvalues, then the nested
+ *     iteration over levels 1..L (exp_bloch2d.c:562-732) -- or, for every
+ *     wave after the first, a warm start from the converged block of the
+ *     k-point one wave earlier (exp_bloch2d.c:814-895, extrapolation 'n');
+ *   - block steps until every wanted pair of every k meets the tolerance:
+ *       PINVIT + Ritz (exp_bloch2d.c:956-1053): defect, prec_steps edge
+ *       V-cycles, update, gradient lifting, Rayleigh-Ritz on the block;
+ *       LOBPCG (test_lobpcg2d.c:217-365 with Knyazev's search direction and
+ *       soft locking): preconditioned defect X, gradient lifting of X,
+ *       Rayleigh-Ritz on [E, X, P] by Cholesky-QR of the Gram matrix.
+ * The coarse solvers are refactored per k (exp_bloch2d.c:782-810) as explicit
+ * inverses.  Residuals are r_i = (A+M) e_i - mu_i M e_i with, as the
+ * stopping rule, either the reference's absolute norm or ||r_i|| / (mu_i ||M e_i||).
+ */
+#include "maxwell_gb300.h"
+#include "mx_internal.h"
+
+#include <cuda_runtime_api.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXL 16
+#define NSTAT 5
+
+struct mxg_solver {
+  mxg_solve_opts o;
+  int n0, L, m, K, pe, pg;
+  cudaStream_t st;
+  cudaEvent_t ev0, ev1;
+  int n[MAXL];
+  double *kd[MAXL];
+  float *kf[MAXL], *kdd[MAXL];
+  double *ph;                        /* K*4 */
+  int *gamma;                        /* K flags */
+  void *b[MAXL], *x[MAXL], *d[MAXL];
+  void *bg[MAXL], *xg[MAXL], *dg[MAXL];
+  double *ae_inv, *an_inv;
+  void *E, *En, *P, *Pn, *Eprev;
+  double *ga, *gm, *coef, *theta, *rwork, *gscratch, *mu, *stats;
+  size_t gscratch_bytes;
+  int *sel, *info;
+  double *cA, *cM, *ccoef, *ctheta, *cwork;   /* coarse eigenproblem */
+  int *cinfo;
+  /* host */
+  double *h_ph, *h_stats, *h_mu, *h_res, *h_rq;
+  int *h_sel, *h_info, *h_conv, *h_steps;
+  int have_prev, K_prev;
+  double last_ms;
+  long launches;
+};
+
+#define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
+#define TRY(x) do { int e_ = (x); if (e_) return e_; } while (0)
+
+static mxk_kappa kap(const mxg_solver *s, int l)
+{
+  mxk_kappa k;
+  k.f = s->kf[l]; k.d = s->kd[l]; k.dd = s->kdd[l];
+  return k;
+}
+
+static size_t elen(const mxg_solver *s, int l) { return (size_t) s->K * 2 * s->n[l] * s->n[l] * s->m; }
+static size_t nlen(const mxg_solver *s, int l) { return (size_t) s->K * s->n[l] * s->n[l] * s->m; }
+
+static int dalloc(void **p, size_t bytes)
+{
+  return cudaMalloc(p, bytes) != cudaSuccess;
+}
+
+void mxg_solver_free(mxg_solver *s)
+{
+  int l;
+  if(!s) return;
+  for(l = 0; l <= s->L; l++) {
+    cudaFree(s->kd[l]); cudaFree(s->kf[l]); cudaFree(s->kdd[l]);
+    cudaFree(s->b[l]); cudaFree(s->x[l]); cudaFree(s->d[l]);
+    cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
+  }
+  cudaFree(s->ph); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv);
+  cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn); cudaFree(s->Eprev);
+  cudaFree(s->ga); cudaFree(s->gm); cudaFree(s->coef); cudaFree(s->theta); cudaFree(s->rwork);
+  cudaFree(s->gscratch); cudaFree(s->mu); cudaFree(s->stats); cudaFree(s->sel); cudaFree(s->info);
+  cudaFree(s->cA); cudaFree(s->cM); cudaFree(s->ccoef); cudaFree(s->ctheta); cudaFree(s->cwork);
+  cudaFree(s->cinfo);
+  if(s->st) cudaStreamDestroy(s->st);
+  if(s->ev0) cudaEventDestroy(s->ev0);
+  if(s->ev1) cudaEventDestroy(s->ev1);
+  free(s->h_ph); free(s->h_stats); free(s->h_mu); free(s->h_res); free(s->h_rq);
+  free(s->h_sel); free(s->h_info); free(s->h_conv); free(s->h_steps);
+  free(s);
+}
+
+mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
+{
+  mxg_solver *s;
+  int l, K, m, ns, N0e, N0n;
+  size_t es_g, es_e;
+  double *kk[MAXL];
+  if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 16
+     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1)
+    return 0;
+  s = calloc(1, sizeof(mxg_solver));
+  s->o = *o;
+  s->n0 = o->n0; s->L = o->L; s->m = m = o->m; s->K = K = o->wave;
+  s->pe = o->precision ? MX_CDD : MX_C128;
+  s->pg = o->precision ? MX_C64 : MX_C128;
+  es_g = mxk_elem_size(s->pg);
+  es_e = mxk_elem_size(s->pe);
+  ns = 3 * m;
+  N0e = 2 * o->n0 * o->n0;
+  N0n = o->n0 * o->n0;
+  if(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) || cudaEventCreate(&s->ev0)
+     || cudaEventCreate(&s->ev1))
+    goto fail;
+  /* kappa hierarchy (coarsen_grid2d, grid2d.c:42-68) */
+  for(l = o->L; l >= 0; l--) {
+    int n = o->n0 << l, i, j;
+    size_t nn = (size_t) n * n, q;
+    float *f, *p;
+    s->n[l] = n;
+    kk[l] = malloc(sizeof(double) * nn);
+    if(l == o->L)
+      memcpy(kk[l], kappa_fine, sizeof(double) * nn);
+    else
+      for(j = 0; j < n; j++)
+        for(i = 0; i < n; i++)
+          kk[l][i + j * n] = 0.25 * (kk[l + 1][2 * i + 2 * j * 2 * n] + kk[l + 1][2 * i + 1 + 2 * j * 2 * n]
+                                     + kk[l + 1][2 * i + (2 * j + 1) * 2 * n]
+                                     + kk[l + 1][2 * i + 1 + (2 * j + 1) * 2 * n]);
+    f = malloc(sizeof(float) * nn);
+    p = malloc(sizeof(float) * 2 * nn);
+    for(q = 0; q < nn; q++) {
+      f[q] = (float) kk[l][q];
+      p[2 * q] = (float) kk[l][q];
+      p[2 * q + 1] = (float) (kk[l][q] - (double) p[2 * q]);
+    }
+    if(dalloc((void **) &s->kd[l], sizeof(double) * nn) || dalloc((void **) &s->kf[l], sizeof(float) * nn)
+       || dalloc((void **) &s->kdd[l], sizeof(float) * 2 * nn)
+       || cudaMemcpy(s->kd[l], kk[l], sizeof(double) * nn, cudaMemcpyHostToDevice)
+       || cudaMemcpy(s->kf[l], f, sizeof(float) * nn, cudaMemcpyHostToDevice)
+       || cudaMemcpy(s->kdd[l], p, sizeof(float) * 2 * nn, cudaMemcpyHostToDevice)) {
+      free(f); free(p);
+      for(; l <= o->L; l++) free(kk[l]);
+      goto fail;
+    }
+    free(f); free(p);
+  }
+  for(l = 0; l <= o->L; l++) free(kk[l]);
+  for(l = 0; l <= o->L; l++)
+    if(dalloc(&s->b[l], elen(s, l) * es_g) || dalloc(&s->x[l], elen(s, l) * es_g) || dalloc(&s->d[l], elen(s, l) * es_g)
+       || dalloc(&s->bg[l], nlen(s, l) * es_g) || dalloc(&s->xg[l], nlen(s, l) * es_g)
+       || dalloc(&s->dg[l], nlen(s, l) * es_g))
+      goto fail;
+  if(dalloc((void **) &s->ph, sizeof(double) * 4 * K) || dalloc((void **) &s->gamma, sizeof(int) * K)
+     || dalloc((void **) &s->ae_inv, sizeof(double) * 2 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->an_inv, sizeof(double) * 2 * (size_t) N0n * N0n * K)
+     || dalloc(&s->E, elen(s, o->L) * es_e) || dalloc(&s->En, elen(s, o->L) * es_e)
+     || dalloc(&s->Eprev, elen(s, o->L) * es_e)
+     || dalloc(&s->P, elen(s, o->L) * es_g) || dalloc(&s->Pn, elen(s, o->L) * es_g)
+     || dalloc((void **) &s->ga, sizeof(double) * 2 * ns * ns * K) || dalloc((void **) &s->gm, sizeof(double) * 2 * ns * ns * K)
+     || dalloc((void **) &s->coef, sizeof(double) * 2 * ns * m * K) || dalloc((void **) &s->theta, sizeof(double) * m * K)
+     || dalloc((void **) &s->rwork, sizeof(double) * 8 * ns * ns * K)
+     || dalloc((void **) &s->mu, sizeof(double) * m * K) || dalloc((void **) &s->stats, sizeof(double) * NSTAT * m * K)
+     || dalloc((void **) &s->sel, sizeof(int) * ns * K) || dalloc((void **) &s->info, sizeof(int) * K)
+     || dalloc((void **) &s->cA, sizeof(double) * 2 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->cM, sizeof(double) * 2 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->ccoef, sizeof(double) * 2 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->ctheta, sizeof(double) * (size_t) N0e * K)
+     || dalloc((void **) &s->cwork, sizeof(double) * 8 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->cinfo, sizeof(int) * K))
+    goto fail;
+  s->gscratch_bytes = (size_t) K * 256 * (ns * (ns + 1) / 2) * 4 * sizeof(double);
+  if(s->gscratch_bytes > ((size_t) 1 << 30)) s->gscratch_bytes = (size_t) 1 << 30;
+  if(dalloc((void **) &s->gscratch, s->gscratch_bytes)) goto fail;
+  s->h_ph = malloc(sizeof(double) * 4 * K);
+  s->h_stats = malloc(sizeof(double) * NSTAT * m * K);
+  s->h_mu = malloc(sizeof(double) * m * K);
+  s->h_res = malloc(sizeof(double) * m * K);
+  s->h_rq = malloc(sizeof(double) * m * K);
+  s->h_sel = malloc(sizeof(int) * ns * K);
+  s->h_info = malloc(sizeof(int) * K);
+  s->h_conv = malloc(sizeof(int) * K);
+  s->h_steps = malloc(sizeof(int) * K);
+  return s;
+fail:
+  mxg_solver_free(s);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+
+static int set_bloch(mxg_solver *s, int K, const mxg_field *xf, const mxg_field *yf)
+{
+  int k, *g = malloc(sizeof(int) * s->K), e;
+  for(k = 0; k < s->K; k++) {
+    int q = k < K ? k : K - 1;   /* unused slots repeat the last k-point */
+    s->h_ph[4 * k] = creal(xf[q]); s->h_ph[4 * k + 1] = cimag(xf[q]);
+    s->h_ph[4 * k + 2] = creal(yf[q]); s->h_ph[4 * k + 3] = cimag(yf[q]);
+    g[k] = xf[q] == 1.0 && yf[q] == 1.0;
+  }
+  e = (int) cudaMemcpyAsync(s->ph, s->h_ph, sizeof(double) * 4 * s->K, cudaMemcpyHostToDevice, s->st);
+  if(!e) e = (int) cudaMemcpyAsync(s->gamma, g, sizeof(int) * s->K, cudaMemcpyHostToDevice, s->st);
+  if(!e) e = (int) cudaStreamSynchronize(s->st);
+  free(g);
+  return e;
+}
+
+/* coarse solvers: explicit inverses of (A+M) on level 0 and of the nodal
+ * Laplace with the k = 0 shift (exp_bloch2d.c:520-528, 799-809) */
+static int factor_coarse(mxg_solver *s)
+{
+  int N0e = 2 * s->n0 * s->n0, N0n = s->n0 * s->n0, k;
+  L_(mxk_dense_edge(s->n0, s->K, s->ph, kap(s, 0), 1.0, 1.0, s->ae_inv, s->st));
+  L_(mxk_hpd_inverse(N0e, s->K, s->ae_inv, s->info, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * s->K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < s->K; k++)
+    if(s->h_info[k]) return MXG_ECONV;
+  L_(mxk_dense_node(s->n0, s->K, s->ph, 1, s->an_inv, s->st));
+  L_(mxk_hpd_inverse(N0n, s->K, s->an_inv, s->info, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * s->K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < s->K; k++)
+    if(s->h_info[k]) return MXG_ECONV;
+  return 0;
+}
+
+/* vcycle_edge2d (edge2d.c:5707-5754) on b[top], x[top] with the coarse inverse */
+static int vcycle_e(mxg_solver *s, int top)
+{
+  int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
+  for(l = top; l > 0; l--) {
+    int n = s->n[l];
+    for(i = 0; i < nu; i++)
+      L_(mxk_edge_gs(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 0, pg, s->b[l], s->x[l], s->st));
+    L_(mxk_convert(pg, s->b[l], pg, s->d[l], elen(s, l), s->st));
+    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->d[l], s->st));
+    L_(mxk_zero(pg, s->b[l - 1], elen(s, l - 1), s->st));
+    L_(mxk_edge_restrict(n / 2, m, K, s->ph, 1.0, pg, s->d[l], s->b[l - 1], s->st));
+    L_(mxk_zero(pg, s->x[l - 1], elen(s, l - 1), s->st));
+  }
+  L_(mxk_coarse_apply(2 * s->n0 * s->n0, m, K, s->ae_inv, pg, s->b[0], s->x[0], 1, s->n0, s->st));
+  for(l = 1; l <= top; l++) {
+    int n = s->n[l];
+    L_(mxk_edge_prolong(n / 2, m, K, s->ph, 1.0, pg, s->x[l - 1], s->x[l], s->st));
+    for(i = 0; i < nu; i++)
+      L_(mxk_edge_gs(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 1, pg, s->b[l], s->x[l], s->st));
+  }
+  return 0;
+}
+
+/* vcycle_node2d (node2d.c:1352-1389) on bg[top], xg[top] */
+static int vcycle_n(mxg_solver *s, int top)
+{
+  int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
+  for(l = top; l > 0; l--) {
+    int n = s->n[l];
+    for(i = 0; i < nu; i++)
+      L_(mxk_node_gs(n, m, K, s->ph, 1.0, 0, pg, s->bg[l], s->xg[l], s->st));
+    L_(mxk_convert(pg, s->bg[l], pg, s->dg[l], nlen(s, l), s->st));
+    L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->dg[l], s->st));
+    L_(mxk_zero(pg, s->bg[l - 1], nlen(s, l - 1), s->st));
+    L_(mxk_node_restrict(n / 2, m, K, s->ph, 1.0, pg, s->dg[l], s->bg[l - 1], s->st));
+    L_(mxk_zero(pg, s->xg[l - 1], nlen(s, l - 1), s->st));
+  }
+  L_(mxk_coarse_apply(s->n0 * s->n0, m, K, s->an_inv, pg, s->bg[0], s->xg[0], 0, s->n0, s->st));
+  for(l = 1; l <= top; l++) {
+    int n = s->n[l];
+    L_(mxk_node_prolong(n / 2, m, K, s->ph, 1.0, pg, s->xg[l - 1], s->xg[l], s->st));
+    for(i = 0; i < nu; i++)
+      L_(mxk_node_gs(n, m, K, s->ph, 1.0, 1, pg, s->bg[l], s->xg[l], s->st));
+  }
+  return 0;
+}
+
+/* gradient lifting (exp_bloch2d.c:971-978): y -= G L^-1 G^H M y */
+static int lift(mxg_solver *s, int l, int py, void *y)
+{
+  int i, n = s->n[l];
+  if(s->o.gradient_steps <= 0) return 0;
+  L_(mxk_adjgradient(n, s->m, s->K, s->ph, 1.0, 1, 0.0, py, y, s->pg, s->bg[l], s->st));
+  L_(mxk_zero(s->pg, s->xg[l], nlen(s, l), s->st));
+  for(i = 0; i < s->o.gradient_steps; i++)
+    TRY(vcycle_n(s, l));
+  L_(mxk_gradient(n, s->m, s->K, s->ph, -1.0, s->pg, s->xg[l], py, y, s->st));
+  return 0;
+}
+
+/* x[l] = V^prec b[l] from zero */
+static int precondition(mxg_solver *s, int l)
+{
+  int i;
+  L_(mxk_zero(s->pg, s->x[l], elen(s, l), s->st));
+  for(i = 0; i < s->o.prec_steps; i++)
+    TRY(vcycle_e(s, l));
+  return 0;
+}
+
+/* residual of E (rhs for the preconditioner into b[l]) and its statistics;
+ * host: residual norms, Rayleigh quotients, convergence per k */
+static int residual(mxg_solver *s, int l, int write_rhs)
+{
+  int k, i, m = s->m, K = s->K;
+  TRY((int) cudaMemsetAsync(s->stats, 0, sizeof(double) * NSTAT * m * K, s->st));
+  L_(mxk_block_residual(s->n[l], m, K, s->ph, kap(s, l), s->mu, s->pe, s->E, s->pg,
+                        write_rhs ? s->b[l] : 0, s->stats, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_stats, s->stats, sizeof(double) * NSTAT * m * K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < K; k++)
+    for(i = 0; i < m; i++) {
+      const double *st = s->h_stats + ((size_t) k * m + i) * NSTAT;
+      double mu = s->h_mu[k * m + i];
+      double r = sqrt(st[0] > 0.0 ? st[0] : 0.0);
+      if(s->o.relative) r /= fabs(mu) * sqrt(st[1]) + 1e-300;
+      s->h_res[k * m + i] = r;
+      s->h_rq[k * m + i] = st[2] / st[3];
+    }
+  return 0;
+}
+
+static int converged_k(const mxg_solver *s, int k)
+{
+  int i;
+  for(i = 0; i < s->o.ieigs; i++)
+    if(!(s->h_res[k * s->m + i] <= s->o.tol))
+      return 0;
+  return 1;
+}
+
+static int upload_mu(mxg_solver *s)
+{
+  return (int) cudaMemcpyAsync(s->mu, s->h_mu, sizeof(double) * s->m * s->K, cudaMemcpyHostToDevice, s->st);
+}
+
+static void swapp(void **a, void **b)
+{
+  void *t = *a;
+  *a = *b;
+  *b = t;
+}
+
+/* Rayleigh-Ritz on the nb blocks (precisions pr, pointers pp) -> coef, theta
+ * with soft locking of converged columns; writes the new E (and P) */
+static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop)
+{
+  int m = s->m, K = s->K, ns = nb * m, k, i, j;
+  L_(mxk_block_gram(s->n[l], m, K, s->ph, kap(s, l), nb, pr, pp, s->ga, s->gm, s->gscratch, s->gscratch_bytes, s->st));
+  for(k = 0; k < K; k++)
+    for(j = 0; j < nb; j++)
+      for(i = 0; i < m; i++)
+        s->h_sel[k * ns + j * m + i] = j == 0 || !(s->h_res[k * m + i] <= s->o.tol);
+  TRY((int) cudaMemcpyAsync(s->sel, s->h_sel, sizeof(int) * ns * K, cudaMemcpyHostToDevice, s->st));
+  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop, s->coef, s->theta, s->info, s->rwork, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_mu, s->theta, sizeof(double) * m * K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < K; k++)
+    if(s->h_info[k] < m) return MXG_ECONV;
+  if(with_p)
+    L_(mxk_block_combine(s->n[l], m, K, nb - 1, pr + 1, pp + 1, s->coef, ns, m, s->pg, s->Pn, s->st));
+  L_(mxk_block_combine(s->n[l], m, K, nb, pr, pp, s->coef, ns, 0, s->pe, s->En, s->st));
+  swapp(&s->E, &s->En);
+  if(with_p) swapp(&s->P, &s->Pn);
+  return upload_mu(s);
+}
+
+static double drop_tol(const mxg_solver *s)
+{
+  return s->o.precision ? 1e-9 : 1e-13;
+}
+
+/* one block step at level l; on entry b[l] holds the residual of E */
+static int block_step(mxg_solver *s, int l, int *have_p)
+{
+  int m = s->m;
+  size_t len = elen(s, l);
+  if(s->o.method == 0) {
+    /* PINVIT: e -= V(defect); center; lift; Ritz on the block */
+    int pr[1];
+    const void *pp[1];
+    TRY(precondition(s, l));
+    L_(mxk_axpy(-1.0, 0.0, s->pg, s->x[l], s->pe, s->E, len, s->st));
+    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->st));
+    TRY(lift(s, l, s->pe, s->E));
+    pr[0] = s->pe; pp[0] = s->E;
+    return ritz(s, l, 1, pr, pp, 0, 1e-14);
+  }
+  else {
+    int pr[3], nb;
+    const void *pp[3];
+    TRY(precondition(s, l));
+    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pg, s->x[l], s->st));
+    TRY(lift(s, l, s->pg, s->x[l]));
+    pr[0] = s->pe; pp[0] = s->E;
+    pr[1] = s->pg; pp[1] = s->x[l];
+    pr[2] = s->pg; pp[2] = s->P;
+    nb = *have_p ? 3 : 2;
+    TRY(ritz(s, l, nb, pr, pp, 1, drop_tol(s)));
+    *have_p = 1;
+    if(s->o.lift_e) {
+      if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->st));
+      TRY(lift(s, l, s->pe, s->E));
+    }
+    return 0;
+  }
+}
+
+/* iterate at level l until all k converge or maxsteps; counts steps per k */
+static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
+{
+  int step, k, have_p = 0, all;
+  for(k = 0; k < s->K; k++) s->h_steps[k] = 0;
+  TRY(residual(s, l, 1));
+  for(step = 0; step < maxsteps; step++) {
+    all = 1;
+    for(k = 0; k < K_active; k++) {
+      s->h_conv[k] = converged_k(s, k);
+      if(!s->h_conv[k]) { all = 0; s->h_steps[k] = step + 1; }
+    }
+    if(all) break;
+    TRY(block_step(s, l, &have_p));
+    TRY(residual(s, l, 1));
+    if(getenv("MXG_DEBUG")) {
+      int i;
+      fprintf(stderr, "level %d step %d:", l, step);
+      for(i = 0; i < s->m; i++) fprintf(stderr, " %.1e", s->h_res[i]);
+      fprintf(stderr, "\n");
+    }
+  }
+  for(k = 0; k < K_active; k++)
+    if(!converged_k(s, k)) s->h_steps[k] = maxsteps;
+  return 0;
+}
+
+/* coarse generalized eigenproblem (exp_bloch2d.c:530-554) and the nested
+ * iteration (exp_bloch2d.c:562-732) for every k of the wave */
+static int cold_start(mxg_solver *s, int K_active)
+{
+  int N = 2 * s->n0 * s->n0, m = s->m, K = s->K, k, i, v, l;
+  double *th = malloc(sizeof(double) * N * K), *cf = malloc(sizeof(double) * 2 * (size_t) N * N * K);
+  double *e0 = malloc(sizeof(double) * 2 * (size_t) K * N * m);
+  int e = 0;
+  L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 1.0, 0.0, s->cA, s->st));
+  L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 0.0, 1.0, s->cM, s->st));
+  L_(mxk_rayleigh_ritz(N, N, K, s->cA, s->cM, 0, 1e-14, s->ccoef, s->ctheta, s->cinfo, s->cwork, s->st));
+  e = (int) cudaMemcpyAsync(th, s->ctheta, sizeof(double) * N * K, cudaMemcpyDeviceToHost, s->st);
+  if(!e) e = (int) cudaMemcpyAsync(cf, s->ccoef, sizeof(double) * 2 * (size_t) N * N * K, cudaMemcpyDeviceToHost, s->st);
+  if(!e) e = (int) cudaStreamSynchronize(s->st);
+  if(e) { free(th); free(cf); free(e0); return e; }
+  /* skip |lambda| < 1e-8 (exp_bloch2d.c:546-551); level-0 block layout of
+   * one k is row-major N x m */
+  for(k = 0; k < K; k++) {
+    int ev;
+    for(ev = 0; ev < N && fabs(th[k * N + ev]) < 1e-8; ev++)
+      ;
+    if(ev + m > N) { free(th); free(cf); free(e0); return MXG_ECONV; }
+    for(v = 0; v < m; v++) {
+      s->h_mu[k * m + v] = 1.0 + th[k * N + ev + v];
+      for(i = 0; i < N; i++) {
+        const double *z = cf + 2 * ((size_t) k * N * N + (size_t) (ev + v) * N + i);
+        double *q = e0 + 2 * (((size_t) k * N + i) * m + v);
+        q[0] = z[0]; q[1] = z[1];
+      }
+    }
+  }
+  /* upload as the level-0 E */
+  {
+    size_t tot = (size_t) K * N * m, o;
+    if(s->pe == MX_C128)
+      e = (int) cudaMemcpy(s->E, e0, sizeof(double) * 2 * tot, cudaMemcpyHostToDevice);
+    else {
+      float *f = malloc(sizeof(float) * 4 * tot);
+      for(o = 0; o < tot; o++) {
+        double re = e0[2 * o], im = e0[2 * o + 1];
+        f[4 * o] = (float) re; f[4 * o + 1] = (float) (re - (double) f[4 * o]);
+        f[4 * o + 2] = (float) im; f[4 * o + 3] = (float) (im - (double) f[4 * o + 2]);
+      }
+      e = (int) cudaMemcpy(s->E, f, sizeof(float) * 4 * tot, cudaMemcpyHostToDevice);
+      free(f);
+    }
+  }
+  free(th); free(cf); free(e0);
+  if(e) return e;
+  TRY(upload_mu(s));
+  for(l = 1; l <= s->L; l++) {
+    L_(mxk_zero(s->pe, s->En, elen(s, l), s->st));
+    L_(mxk_edge_prolong(s->n[l - 1], m, K, s->ph, 1.0, s->pe, s->E, s->En, s->st));
+    swapp(&s->E, &s->En);
+    /* Rayleigh quotients of the prolongated vectors (exp_bloch2d.c:567-583) */
+    TRY(residual(s, l, 0));
+    for(k = 0; k < K * m; k++) s->h_mu[k] = s->h_rq[k];
+    TRY(upload_mu(s));
+    TRY(iterate(s, l, l == s->L ? s->o.max_steps : s->o.max_nested, K_active));
+  }
+  return 0;
+}
+
+int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field *yf, double *lambda,
+                    int *steps, double *res)
+{
+  int w, k, i, m = s->m, K = s->K;
+  float ms;
+  double total = 0.0;
+  s->launches = 0;
+  for(w = 0; w * K < nk; w++) {
+    int k0 = w * K, Ka = nk - k0 < K ? nk - k0 : K;
+    TRY(set_bloch(s, Ka, xf + k0, yf + k0));
+    TRY((int) cudaEventRecord(s->ev0, s->st));
+    TRY(factor_coarse(s));
+    if(!s->have_prev || s->K_prev != K) {
+      TRY(cold_start(s, Ka));
+    }
+    else {
+      /* warm start from the k-point one wave earlier (extrapolation 'n') */
+      L_(mxk_convert(s->pe, s->Eprev, s->pe, s->E, elen(s, s->L), s->st));
+      TRY(residual(s, s->L, 0));
+      for(k = 0; k < K * m; k++) s->h_mu[k] = s->h_rq[k];
+      TRY(upload_mu(s));
+      TRY(iterate(s, s->L, s->o.max_steps, Ka));
+    }
+    TRY((int) cudaEventRecord(s->ev1, s->st));
+    TRY((int) cudaEventSynchronize(s->ev1));
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    total += ms;
+    for(k = 0; k < Ka; k++) {
+      if(steps) steps[k0 + k] = s->h_steps[k];
+      for(i = 0; i < m; i++) {
+        if(lambda) lambda[(size_t) (k0 + k) * m + i] = s->h_rq[k * m + i] - 1.0;
+        if(res) res[(size_t) (k0 + k) * m + i] = s->h_res[k * m + i];
+      }
+    }
+    L_(mxk_convert(s->pe, s->E, s->pe, s->Eprev, elen(s, s->L), s->st));
+    s->have_prev = 1;
+    s->K_prev = K;
+  }
+  s->last_ms = total;
+  return (int) cudaStreamSynchronize(s->st);
+}
+
+int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host)
+{
+  size_t per = 2 * (size_t) s->n[s->L] * s->n[s->L], tot = (size_t) s->K * s->m * per, es = mxk_elem_size(s->pe);
+  size_t k, v, e;
+  unsigned char *buf = malloc(es * tot);
+  double *h = (double *) host;
+  int err = (int) cudaMemcpy(buf, s->E, es * tot, cudaMemcpyDeviceToHost);
+  for(k = 0; !err && k < (size_t) s->K; k++)
+    for(v = 0; v < (size_t) s->m; v++)
+      for(e = 0; e < per; e++) {
+        size_t o = (k * per + e) * s->m + v;
+        double *z = h + 2 * ((k * s->m + v) * per + e);
+        if(s->pe == MX_C128) {
+          z[0] = ((double *) buf)[2 * o]; z[1] = ((double *) buf)[2 * o + 1];
+        }
+        else {
+          const float *q = (const float *) buf + 4 * o;
+          z[0] = (double) q[0] + (double) q[1];
+          z[1] = (double) q[2] + (double) q[3];
+        }
+      }
+  free(buf);
+  return err;
+}
+
+int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches)
+{
+  if(ms) *ms = s->last_ms;
+  if(launches) *launches = s->launches;
+  return 0;
+}
+
+int mxg_eps_sensitivity(int n, const double *kappa, int nk, const mxg_field *xf, const mxg_field *yf, int m,
+                        const mxg_field *evec, const double *weights, double *grad)
+{
+  grid2d_gpu *g;
+  edge2d_gpu *e;
+  double *dk, *dw, *dg;
+  int err;
+  if(m < 1 || m > 32) return MXG_EINVAL;
+  g = new_grid2d_gpu(n, n, 1.0 / n, 1.0 / n, nk);
+  if(!g) return MXG_ENOMEM;
+  err = setkappa_grid2d_gpu(g, kappa);
+  if(!err) err = setbloch_grid2d_gpu(g, xf, yf);
+  e = err ? 0 : new_edge2d_gpu(g, m, MXG_C128);
+  if(!e) { del_grid2d_gpu(g); return err ? err : MXG_ENOMEM; }
+  err = denseto_edge2d_gpu(evec, e);
+  if(cudaMalloc((void **) &dk, sizeof(double) * n * n)) { del_edge2d_gpu(e); del_grid2d_gpu(g); return MXG_ENOMEM; }
+  if(cudaMalloc((void **) &dw, sizeof(double) * nk * m)) { cudaFree(dk); del_edge2d_gpu(e); del_grid2d_gpu(g); return MXG_ENOMEM; }
+  if(cudaMalloc((void **) &dg, sizeof(double) * n * n)) { cudaFree(dk); cudaFree(dw); del_edge2d_gpu(e); del_grid2d_gpu(g); return MXG_ENOMEM; }
+  if(!err) err = (int) cudaMemcpy(dk, kappa, sizeof(double) * n * n, cudaMemcpyHostToDevice);
+  if(!err) err = (int) cudaMemcpy(dw, weights, sizeof(double) * nk * m, cudaMemcpyHostToDevice);
+  if(!err) err = mxk_eps_sensitivity(n, m, nk, mxg__grid_phases(g), dk, dw, MX_C128, mxg__edge_data(e), dg, 0);
+  if(!err) err = (int) cudaMemcpy(grad, dg, sizeof(double) * n * n, cudaMemcpyDeviceToHost);
+  cudaFree(dk); cudaFree(dw); cudaFree(dg);
+  del_edge2d_gpu(e);
+  del_grid2d_gpu(g);
+  return err;
+}
