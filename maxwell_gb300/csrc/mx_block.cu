@@ -150,6 +150,8 @@ struct GramArgs {
   mxk_kappa kap;
   int chunks;              // CTAs per k
   double* partial;         // [K][chunks][nent][4]  (ga re, ga im, gm re, gm im)
+  const float2* resid;     // optional c64 residual r_j of the high columns (see below)
+  const double* theta;     // their Ritz values
 };
 
 __device__ __forceinline__ cx<float> ld_any_f(int prec, const void* base, size_t off) {
@@ -172,6 +174,8 @@ __global__ void k_block_gram(GramArgs a, int mh) {
   cx<float>* lo = reinterpret_cast<cx<float>*>(hi + TS * mh * 5);      // TS*ns*5
   HI* kap_h = reinterpret_cast<HI*>(lo + TS * ns * 5);                // TS
   float* kap_t = reinterpret_cast<float*>(kap_h + TS);                // TS
+  cx<float>* rs = reinterpret_cast<cx<float>*>(kap_t + TS);          // TS*mh*2 (x, y of r)
+  bool use_r = a.resid != nullptr;
   Seam<float> sf = seam_of<float>(a.ph, k, n);
   Seam<HI> sh = seam_of<HI>(a.ph, k, n);
   constexpr int MAXE = 5;   // ns <= 48 -> nent <= 1176 <= 5*256
@@ -243,6 +247,16 @@ __global__ void k_block_gram(GramArgs a, int mh) {
         ls[4] = scal(mmf, scal(4.0f, y0) + X(1, i + 1, j) + X(1, i - 1, j));
       }
     }
+    if (use_r)
+      for (int w = threadIdx.x; w < TS * mh; w += GT) {
+        int ts = w / mh, v = w % mh;
+        size_t site = base + ts;
+        if (site >= s1) continue;
+        int i = (int) (site % n), j = (int) (site / n);
+        float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
+        rs[((size_t) ts * mh + v) * 2] = mkc(rx.x, rx.y);
+        rs[((size_t) ts * mh + v) * 2 + 1] = mkc(ry.x, ry.y);
+      }
     for (int ts = threadIdx.x; ts < TS; ts += GT) {
       size_t site = base + ts;
       if (site < s1) {
@@ -267,6 +281,18 @@ __global__ void k_block_gram(GramArgs a, int mh) {
         }
         hacc_a[t] += sa;
         hacc_m[t] += sm2;
+      } else if (use_r && j < mh) {
+        // cross entry s_i^H (A+M) e_j = theta_j s_i^H M e_j + s_i^H r_j: only
+        // s_i^H r_j is accumulated here, the rest is added at the end
+        cx<float> sa = czero<float>(), sm2 = czero<float>();
+        for (int ts = 0; ts < nts; ts++) {
+          const cx<float>* ls = lo + (size_t) ts * ns * 5;
+          const cx<float>* rr = rs + (size_t) ts * mh * 2;
+          sa += conjc(ls[i * 5 + 1]) * rr[j * 2] + conjc(ls[i * 5 + 2]) * rr[j * 2 + 1];
+          sm2 += conjc(ls[i * 5 + 1]) * ls[j * 5 + 3] + conjc(ls[i * 5 + 2]) * ls[j * 5 + 4];
+        }
+        acc_a[t] += sa;
+        acc_m[t] += sm2;
       } else {
         cx<float> sa = czero<float>(), sm2 = czero<float>();
         for (int ts = 0; ts < nts; ts++) {
@@ -288,9 +314,16 @@ __global__ void k_block_gram(GramArgs a, int mh) {
     double ai = Real<HI>::to_double(hacc_a[t].im) + (double) acc_a[t].im;
     double mr = Real<HI>::to_double(hacc_m[t].re) + (double) acc_m[t].re;
     double mi = Real<HI>::to_double(hacc_m[t].im) + (double) acc_m[t].im;
-    // A + M = axy * (sum over cells of kappa conj(curl_i) curl_j) + M
-    out[(size_t) e * 4 + 0] = axy * ar + mr;
-    out[(size_t) e * 4 + 1] = axy * ai + mi;
+    // A + M = axy * (sum over cells of kappa conj(curl_i) curl_j) + M, or
+    // for the residual form of the cross entries theta_j * M + s_i^H r_j
+    if (use_r && ei[t] >= mh && ej[t] < mh) {
+      double th = a.theta[(size_t) k * m + ej[t]];
+      out[(size_t) e * 4 + 0] = th * mr + ar;
+      out[(size_t) e * 4 + 1] = th * mi + ai;
+    } else {
+      out[(size_t) e * 4 + 0] = axy * ar + mr;
+      out[(size_t) e * 4 + 1] = axy * ai + mi;
+    }
     out[(size_t) e * 4 + 2] = mr;
     out[(size_t) e * 4 + 3] = mi;
   }
@@ -432,8 +465,8 @@ static int gram_chunks(int K, size_t nsite) {
 }
 
 extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa kap, int nb, const int* precs,
-                              const void* const* ptrs, double* ga, double* gm, double* scratch,
-                              size_t scratch_bytes, mx_stream s) {
+                              const void* const* ptrs, const void* resid, const double* theta, double* ga,
+                              double* gm, double* scratch, size_t scratch_bytes, mx_stream s) {
   if (nb < 1 || nb > 4 || nb * m > 48) return (int) cudaErrorInvalidValue;
   GramArgs a;
   a.n = n; a.m = m; a.K = K; a.nb = nb; a.ns = nb * m;
@@ -442,6 +475,8 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
     a.ptrs[b] = b < nb ? ptrs[b] : nullptr;
   }
   a.ph = ph; a.kap = kap;
+  a.resid = (const float2*) resid;
+  a.theta = theta;
   int nent = a.ns * (a.ns + 1) / 2;
   a.chunks = gram_chunks(K, (size_t) n * n);
   size_t need = (size_t) K * a.chunks * nent * 4 * sizeof(double);
@@ -458,7 +493,9 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
   bool hi_dd = precs[0] == MX_CDD;
   int mh = all128 ? a.ns : (precs[0] == MX_C64 ? 0 : m);
   size_t hsz = hi_dd ? sizeof(cx<dd>) : sizeof(cx<double>);
-  size_t smem = hsz * TS * mh * 5 + sizeof(cx<float>) * TS * a.ns * 5 + (hsz / 2 + sizeof(float)) * TS + 16;
+  if (resid && (all128 || mh == 0)) return (int) cudaErrorInvalidValue;
+  size_t smem = hsz * TS * mh * 5 + sizeof(cx<float>) * TS * a.ns * 5 + (hsz / 2 + sizeof(float)) * TS
+                + sizeof(cx<float>) * TS * mh * 2 + 16;
   if (hi_dd) {
     cudaFuncSetAttribute(k_block_gram<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     k_block_gram<dd><<<g, GT, smem, st>>>(a, mh);

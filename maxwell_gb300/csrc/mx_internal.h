@@ -105,9 +105,14 @@ int mxk_block_residual(int n, int m, int K, const double *phases, mxk_kappa kap,
                        double *stats, mx_stream s);
 /* Gram matrices of the basis S = [blocks...]: nb blocks of m vectors each,
  * block b with precision precs[b] at ptrs[b].  ga = S^H (A+M) S, gm = S^H M S,
- * full ns x ns (ns = nb*m) per k, column-major, complex double. */
+ * full ns x ns (ns = nb*m) per k, column-major, complex double.
+ * With resid (c64, the residuals r_j = (A+M) e_j - theta_j M e_j of the first
+ * block, a float-float block) the entries between a low column s_i and e_j
+ * are formed as theta_j s_i^H M e_j + s_i^H r_j, which keeps
+ * ga - theta gm free of the cancellation that FP32 products would suffer. */
 int mxk_block_gram(int n, int m, int K, const double *phases, mxk_kappa kap, int nb,
-                   const int *precs, const void *const *ptrs, double *ga, double *gm,
+                   const int *precs, const void *const *ptrs, const void *resid,
+                   const double *theta, double *ga, double *gm,
                    double *scratch, size_t scratch_bytes, mx_stream s);
 /* out_j = sum_i coef(i,j) S_i for the blocks listed; coef is ns x m per k,
  * only rows [row0, row0 + nb*m) are used */

@@ -351,7 +351,11 @@ static void swapp(void **a, void **b)
 static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop)
 {
   int m = s->m, K = s->K, ns = nb * m, k, i, j;
-  L_(mxk_block_gram(s->n[l], m, K, s->ph, kap(s, l), nb, pr, pp, s->ga, s->gm, s->gscratch, s->gscratch_bytes, s->st));
+  /* the residual of E sits in b[l] (written by residual()) with the Ritz
+   * values mu; the mixed solver forms the E-to-search-block entries from it */
+  const void *rr = (s->pe == MX_CDD && nb > 1) ? s->b[l] : 0;
+  L_(mxk_block_gram(s->n[l], m, K, s->ph, kap(s, l), nb, pr, pp, rr, s->mu, s->ga, s->gm, s->gscratch,
+                    s->gscratch_bytes, s->st));
   for(k = 0; k < K; k++)
     for(j = 0; j < nb; j++)
       for(i = 0; i < m; i++)
@@ -373,7 +377,9 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
 
 static double drop_tol(const mxg_solver *s)
 {
-  return s->o.precision ? 1e-9 : 1e-13;
+  const char *e = getenv("MXG_DROP");
+  if(e) return atof(e);
+  return s->o.precision ? 1e-6 : 1e-12;
 }
 
 /* one block step at level l; on entry b[l] holds the residual of E */
@@ -429,7 +435,7 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
     TRY(residual(s, l, 1));
     if(getenv("MXG_DEBUG")) {
       int i;
-      fprintf(stderr, "level %d step %d:", l, step);
+      fprintf(stderr, "level %d step %d rank %d:", l, step, s->h_info[0]);
       for(i = 0; i < s->m; i++) fprintf(stderr, " %.1e", s->h_res[i]);
       fprintf(stderr, "\n");
     }
