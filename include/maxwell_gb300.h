@@ -169,6 +169,11 @@ int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of
  * kernel launches it issued */
 int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches);
+/* CUDA-event timing of the finest-level AFW Gauss-Seidel sweeps: total
+ * milliseconds and number of sweeps since profiling was enabled, and the
+ * algorithmic bytes of one sweep (x, b, kappa read once, x written once) */
+int mxg_solver_profile(mxg_solver *s, int enable);
+int mxg_solver_kernel_time(mxg_solver *s, double *ms, long *count, double *bytes_per_sweep);
 
 /* ---------- eigenvalue sensitivity (no counterpart in the reference) ---------- */
 /* grad[c] = sum_{k,v} w[k*m+v] d lambda_{k,v} / d eps_c for M-normalised

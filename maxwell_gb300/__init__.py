@@ -99,6 +99,8 @@ def lib() -> C.CDLL:
             "mxg_bloch_solve": (I, [P, I, P, P, P, P, P]),
             "mxg_solver_eigenvectors": (I, [P, P]),
             "mxg_solver_stats": (I, [P, P, P]),
+            "mxg_solver_profile": (I, [P, I]),
+            "mxg_solver_kernel_time": (I, [P, P, P, P]),
             "mxg_eps_sensitivity": (I, [I, P, I, P, P, I, P, P, P]),
             "mxg_device_ok": (I, []),
         }
@@ -273,6 +275,14 @@ class Solver:
         ms, launches = C.c_double(0), C.c_long(0)
         lib().mxg_solver_stats(self.h, C.byref(ms), C.byref(launches))
         return ms.value, launches.value
+
+    def profile(self, enable: bool = True):
+        check(lib().mxg_solver_profile(self.h, int(enable)), "profile")
+
+    def kernel_time(self):
+        ms, cnt, b = C.c_double(0), C.c_long(0), C.c_double(0)
+        check(lib().mxg_solver_kernel_time(self.h, C.byref(ms), C.byref(cnt), C.byref(b)), "kernel_time")
+        return ms.value, cnt.value, b.value
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

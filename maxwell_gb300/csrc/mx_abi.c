@@ -27,7 +27,8 @@ struct grid2d_gpu {
   double *kd;          /* device kappa, double */
   float *kf;           /* float */
   float *kdd;          /* float-float pairs */
-  double *ph;          /* device phases K*4 */
+  void *afw;           /* AFW patch factors for alpha = beta = 1 */
+  double *ph;          /* device phase table (mxk_phase_bytes) */
   double *h_kappa;     /* host copies */
   double *h_ph;
   cudaStream_t st;
@@ -58,6 +59,9 @@ static mxk_kappa kap_of(const grid2d_gpu *g)
   k.f = g->kf;
   k.d = g->kd;
   k.dd = g->kdd;
+  k.afw = g->afw;
+  k.afw_alpha = 1.0;
+  k.afw_beta = 1.0;
   return k;
 }
 
@@ -75,6 +79,8 @@ static int upload_kappa(grid2d_gpu *g)
   e = (int) cudaMemcpy(g->kd, g->h_kappa, sizeof(double) * nn, cudaMemcpyHostToDevice);
   if(!e) e = (int) cudaMemcpy(g->kf, f, sizeof(float) * nn, cudaMemcpyHostToDevice);
   if(!e) e = (int) cudaMemcpy(g->kdd, p, sizeof(float) * 2 * nn, cudaMemcpyHostToDevice);
+  if(!e) e = mxk_afw_factors(g->n, g->kf, 1.0, 1.0, g->afw, g->st);
+  if(!e) e = (int) cudaStreamSynchronize(g->st);
   free(f);
   free(p);
   return e;
@@ -87,20 +93,21 @@ static grid2d_gpu *alloc_grid(int n, int K, cudaStream_t st)
   int k;
   g->n = n; g->K = K; g->h = 1.0 / n;
   g->h_kappa = malloc(sizeof(double) * nn);
-  g->h_ph = malloc(sizeof(double) * 4 * K);
+  g->h_ph = malloc(mxk_phase_bytes(K));
   for(k = 0; k < (int) nn; k++) g->h_kappa[k] = 1.0;
   for(k = 0; k < K; k++) {
     g->h_ph[4 * k] = 1.0; g->h_ph[4 * k + 1] = 0.0;
     g->h_ph[4 * k + 2] = 1.0; g->h_ph[4 * k + 3] = 0.0;
   }
   if(cudaMalloc((void **) &g->kd, sizeof(double) * nn) || cudaMalloc((void **) &g->kf, sizeof(float) * nn)
-     || cudaMalloc((void **) &g->kdd, sizeof(float) * 2 * nn)
-     || cudaMalloc((void **) &g->ph, sizeof(double) * 4 * K)) {
+     || cudaMalloc((void **) &g->kdd, sizeof(float) * 2 * nn) || cudaMalloc(&g->afw, 32 * nn)
+     || cudaMalloc((void **) &g->ph, mxk_phase_bytes(K))) {
     free(g->h_kappa); free(g->h_ph); free(g);
     return 0;
   }
   g->st = st;
-  if(upload_kappa(g) || cudaMemcpy(g->ph, g->h_ph, sizeof(double) * 4 * K, cudaMemcpyHostToDevice)) {
+  mxk_phase_fill(K, g->h_ph);
+  if(upload_kappa(g) || cudaMemcpy(g->ph, g->h_ph, mxk_phase_bytes(K), cudaMemcpyHostToDevice)) {
     del_grid2d_gpu(g);
     return 0;
   }
@@ -118,7 +125,7 @@ grid2d_gpu *new_grid2d_gpu(int nx, int ny, double hx, double hy, int K)
 void del_grid2d_gpu(grid2d_gpu *g)
 {
   if(!g) return;
-  cudaFree(g->kd); cudaFree(g->kf); cudaFree(g->kdd); cudaFree(g->ph);
+  cudaFree(g->kd); cudaFree(g->kf); cudaFree(g->kdd); cudaFree(g->afw); cudaFree(g->ph);
   free(g->h_kappa); free(g->h_ph);
   free(g);
 }
@@ -135,8 +142,8 @@ grid2d_gpu *coarsen_grid2d_gpu(const grid2d_gpu *f)
       g->h_kappa[i + j * n] = 0.25 * (f->h_kappa[2 * i + 2 * j * 2 * n] + f->h_kappa[2 * i + 1 + 2 * j * 2 * n]
                                       + f->h_kappa[2 * i + (2 * j + 1) * 2 * n]
                                       + f->h_kappa[2 * i + 1 + (2 * j + 1) * 2 * n]);
-  memcpy(g->h_ph, f->h_ph, sizeof(double) * 4 * f->K);
-  if(upload_kappa(g) || cudaMemcpy(g->ph, g->h_ph, sizeof(double) * 4 * g->K, cudaMemcpyHostToDevice)) {
+  memcpy(g->h_ph, f->h_ph, mxk_phase_bytes(f->K));
+  if(upload_kappa(g) || cudaMemcpy(g->ph, g->h_ph, mxk_phase_bytes(g->K), cudaMemcpyHostToDevice)) {
     del_grid2d_gpu(g);
     return 0;
   }
@@ -156,7 +163,8 @@ int setbloch_grid2d_gpu(grid2d_gpu *g, const mxg_field *xf, const mxg_field *yf)
     g->h_ph[4 * k] = creal_(xf[k]); g->h_ph[4 * k + 1] = cimag_(xf[k]);
     g->h_ph[4 * k + 2] = creal_(yf[k]); g->h_ph[4 * k + 3] = cimag_(yf[k]);
   }
-  return (int) cudaMemcpy(g->ph, g->h_ph, sizeof(double) * 4 * g->K, cudaMemcpyHostToDevice);
+  mxk_phase_fill(g->K, g->h_ph);
+  return (int) cudaMemcpy(g->ph, g->h_ph, mxk_phase_bytes(g->K), cudaMemcpyHostToDevice);
 }
 
 int getsize_grid2d_gpu(const grid2d_gpu *g, int *nx, int *K)
@@ -308,12 +316,15 @@ int norm2_edge2d_gpu(const edge2d_gpu *x, double *out)
 int center_edge2d_gpu(edge2d_gpu *x)
 {
   int K = x->gr->K, k, e, *flags, *d;
+  double *acc;
   flags = malloc(sizeof(int) * K);
   for(k = 0; k < K; k++) flags[k] = 1;
   if(cudaMalloc((void **) &d, sizeof(int) * K)) { free(flags); return MXG_ENOMEM; }
+  if(cudaMalloc((void **) &acc, sizeof(double) * 4 * K * x->m)) { cudaFree(d); free(flags); return MXG_ENOMEM; }
   e = (int) cudaMemcpy(d, flags, sizeof(int) * K, cudaMemcpyHostToDevice);
-  if(!e) e = mxk_center(x->gr->n, x->m, K, d, x->prec, x->d, x->gr->st);
+  if(!e) e = mxk_center(x->gr->n, x->m, K, d, x->prec, x->d, acc, x->gr->st);
   if(!e) e = (int) cudaStreamSynchronize(x->gr->st);
+  cudaFree(acc);
   cudaFree(d);
   free(flags);
   return e;
@@ -324,7 +335,7 @@ int addeval_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *x, edg
   const grid2d_gpu *g = x->gr;
   if(!same_shape_e(x, y) || cimag_(alpha) != 0.0 || cimag_(beta) != 0.0) return MXG_EINVAL;
   return mxk_edge_apply(g->n, x->m, g->K, g->ph, kap_of(g), creal_(alpha), creal_(beta), 0, 1.0,
-                        x->prec, x->d, y->prec, y->d, g->st);
+                        x->prec, x->d, y->prec, 0, y->d, g->st);
 }
 
 int addeval_shifted_edge2d_gpu(double alpha, const double *beta, const edge2d_gpu *x, edge2d_gpu *y)
@@ -336,7 +347,8 @@ int addeval_shifted_edge2d_gpu(double alpha, const double *beta, const edge2d_gp
   if(!same_shape_e(x, y)) return MXG_EINVAL;
   if(cudaMalloc((void **) &d, sizeof(double) * km)) return MXG_ENOMEM;
   e = (int) cudaMemcpy(d, beta, sizeof(double) * km, cudaMemcpyHostToDevice);
-  if(!e) e = mxk_edge_apply(g->n, x->m, g->K, g->ph, kap_of(g), alpha, 0.0, d, 1.0, x->prec, x->d, y->prec, y->d, g->st);
+  if(!e) e = mxk_edge_apply(g->n, x->m, g->K, g->ph, kap_of(g), alpha, 0.0, d, 1.0, x->prec, x->d, y->prec, 0, y->d,
+                            g->st);
   if(!e) e = (int) cudaStreamSynchronize(g->st);
   cudaFree(d);
   return e;
@@ -350,7 +362,7 @@ static int product_e(double alpha, double beta, const edge2d_gpu *x, const edge2
   int e;
   if(!t) { free(buf); return MXG_ENOMEM; }
   e = mxk_edge_apply(x->gr->n, x->m, x->gr->K, x->gr->ph, kap_of(x->gr), alpha, beta, 0, 0.0, y->prec, y->d,
-                     t->prec, t->d, x->gr->st);
+                     t->prec, 0, t->d, x->gr->st);
   if(!e) {
     edge2d_gpu xx = *x;
     if(x->prec != t->prec) e = MXG_EINVAL;
@@ -408,9 +420,9 @@ int vcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2
     const grid2d_gpu *g = x[l]->gr;
     for(i = 0; i < nu; i++)
       TRY(mxk_edge_gs(g->n, x[l]->m, g->K, g->ph, kap_of(g), 1.0, 1.0, 0, x[l]->prec, b[l]->d, x[l]->d, g->st));
-    TRY(copy_edge2d_gpu(b[l], d[l]));
+    if(b[l]->prec != d[l]->prec) return MXG_EINVAL;
     TRY(mxk_edge_apply(g->n, x[l]->m, g->K, g->ph, kap_of(g), -1.0, -1.0, 0, 1.0, x[l]->prec, x[l]->d,
-                       d[l]->prec, d[l]->d, g->st));
+                       d[l]->prec, b[l]->d, d[l]->d, g->st));
     TRY(zero_edge2d_gpu(b[l - 1]));
     TRY(mxk_edge_restrict(g->n / 2, x[l]->m, g->K, g->ph, 1.0, d[l]->prec, d[l]->d, b[l - 1]->d, g->st));
     TRY(zero_edge2d_gpu(x[l - 1]));
@@ -418,7 +430,7 @@ int vcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2
   if(Ac) {
     const grid2d_gpu *g = x[0]->gr;
     if(!Ac->factored || Ac->rows != 2 * g->n * g->n || Ac->K != g->K) return MXG_EINVAL;
-    TRY(mxk_coarse_apply(Ac->rows, x[0]->m, g->K, Ac->d, x[0]->prec, b[0]->d, x[0]->d, 1, g->n, g->st));
+    TRY(mxk_coarse_apply(Ac->rows, x[0]->m, g->K, Ac->d, 0, x[0]->prec, b[0]->d, x[0]->d, g->st));
   }
   else
     for(i = 0; i < nu; i++)
@@ -481,14 +493,17 @@ int addeval_node2d_gpu(mxg_field alpha, const node2d_gpu *x, node2d_gpu *y)
 {
   const grid2d_gpu *g = x->gr;
   if(x->prec != y->prec || x->m != y->m) return MXG_EINVAL;
-  return mxk_node_apply(g->n, x->m, g->K, g->ph, creal_(alpha), 1.0, x->prec, x->d, y->d, g->st);
+  return mxk_node_apply(g->n, x->m, g->K, g->ph, creal_(alpha), 1.0, x->prec, x->d, 0, y->d, g->st);
 }
 
 static int gs_n(double a, const node2d_gpu *b, node2d_gpu *x, int dir)
 {
   const grid2d_gpu *g = x->gr;
+  int e;
   if(b->prec != x->prec || b->m != x->m) return MXG_EINVAL;
-  return mxk_node_gs(g->n, x->m, g->K, g->ph, a, dir, x->prec, b->d, x->d, g->st);
+  e = mxk_node_gs(g->n, x->m, g->K, g->ph, a, dir, x->prec, b->d, x->d, g->st);
+  if(!e) e = (int) cudaStreamSynchronize(g->st);
+  return e;
 }
 
 int gsforward_node2d_gpu(mxg_field a, const node2d_gpu *b, node2d_gpu *x) { return gs_n(creal_(a), b, x, 0); }
@@ -527,9 +542,9 @@ int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2
   for(l = L; l > 0; l--) {
     const grid2d_gpu *g = x[l]->gr;
     for(i = 0; i < nu; i++)
-      TRY(mxk_node_gs(g->n, x[l]->m, g->K, g->ph, 1.0, 0, x[l]->prec, b[l]->d, x[l]->d, g->st));
-    TRY(mxk_convert(b[l]->prec, b[l]->d, d[l]->prec, d[l]->d, nlen(b[l]), g->st));
-    TRY(mxk_node_apply(g->n, x[l]->m, g->K, g->ph, -1.0, 1.0, x[l]->prec, x[l]->d, d[l]->d, g->st));
+      TRY(gs_n(1.0, b[l], x[l], 0));
+    if(b[l]->prec != d[l]->prec) return MXG_EINVAL;
+    TRY(mxk_node_apply(g->n, x[l]->m, g->K, g->ph, -1.0, 1.0, x[l]->prec, x[l]->d, b[l]->d, d[l]->d, g->st));
     TRY(zero_node2d_gpu(b[l - 1]));
     TRY(mxk_node_restrict(g->n / 2, x[l]->m, g->K, g->ph, 1.0, d[l]->prec, d[l]->d, b[l - 1]->d, g->st));
     TRY(zero_node2d_gpu(x[l - 1]));
@@ -537,7 +552,7 @@ int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2
   if(Ac) {
     const grid2d_gpu *g = x[0]->gr;
     if(!Ac->factored || Ac->rows != g->n * g->n || Ac->K != g->K) return MXG_EINVAL;
-    TRY(mxk_coarse_apply(Ac->rows, x[0]->m, g->K, Ac->d, x[0]->prec, b[0]->d, x[0]->d, 0, g->n, g->st));
+    TRY(mxk_coarse_apply(Ac->rows, x[0]->m, g->K, Ac->d, 0, x[0]->prec, b[0]->d, x[0]->d, g->st));
   }
   else
     for(i = 0; i < nu; i++)
@@ -546,7 +561,7 @@ int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2
     const grid2d_gpu *g = x[l]->gr;
     TRY(mxk_node_prolong(g->n / 2, x[l]->m, g->K, g->ph, 1.0, x[l]->prec, x[l - 1]->d, x[l]->d, g->st));
     for(i = 0; i < nu; i++)
-      TRY(mxk_node_gs(g->n, x[l]->m, g->K, g->ph, 1.0, 1, x[l]->prec, b[l]->d, x[l]->d, g->st));
+      TRY(gs_n(1.0, b[l], x[l], 1));
   }
   return (int) cudaStreamSynchronize(x[L]->gr->st);
 }
@@ -641,7 +656,7 @@ int sygv_matrix_gpu(matrix_gpu *a, matrix_gpu *b, double *lambda, int *info)
   }
   /* the Ritz kernel reads full Hermitian matrices: complete from the lower triangle on the host side
    * of the convention (callers pass full matrices, as densematrix_*_gpu produces) */
-  e = mxk_rayleigh_ritz(N, N, K, a->d, b->d, 0, 1e-14, coef, theta, a->info, work, 0);
+  e = mxk_rayleigh_ritz(N, N, K, a->d, b->d, 0, 1e-14, -1e300, coef, theta, a->info, work, 0);
   if(!e) e = (int) cudaMemcpy(lambda, theta, sizeof(double) * (size_t) N * K, cudaMemcpyDeviceToHost);
   if(!e) e = (int) cudaMemcpy(info, a->info, sizeof(int) * K, cudaMemcpyDeviceToHost);
   if(!e) e = (int) cudaMemcpy(a->d, coef, sizeof(double) * 2 * (size_t) N * N * K, cudaMemcpyDeviceToDevice);

@@ -22,14 +22,6 @@ using namespace mx;
 
 namespace {
 
-template <typename R>
-__device__ __forceinline__ Seam<R> seam_of(const double* ph, int k, int n) {
-  Seam<R> s;
-  s.xf = cfrom<R>(ph[4 * k + 0], ph[4 * k + 1]);
-  s.yf = cfrom<R>(ph[4 * k + 2], ph[4 * k + 3]);
-  s.n = n;
-  return s;
-}
 
 template <typename S, typename R>
 struct EA {
@@ -44,7 +36,6 @@ struct EA {
   }
 };
 
-template <typename R> __device__ __forceinline__ R rf(double d) { return Real<R>::from(d); }
 
 template <typename R> struct KapB;
 template <> struct KapB<float> {
@@ -78,23 +69,27 @@ __device__ __forceinline__ cx<R> curlc(const A& E, int i, int j) {
 constexpr int NSTAT = 5;
 
 template <typename SE, typename SR, typename R>
-__global__ void k_block_residual(int n, int m, int K, const double* __restrict__ ph, KapB<R> kap,
-                                 const double* __restrict__ mu, const SE* __restrict__ e,
+__global__ void k_block_residual(int n, int m, int K, const double* __restrict__ ph, KapB<R> kap, Sc axy_s,
+                                 Sc sixth, const double* __restrict__ mu, const SE* __restrict__ e,
                                  SR* __restrict__ rout, double* __restrict__ stats) {
   // block: m lanes (v) x rows; grid (G, K)
   int k = blockIdx.y;
   int v = threadIdx.x % m, row = threadIdx.x / m, rows = blockDim.x / m;
   Lay L{n, m, K};
-  EA<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, seam_of<R>(ph, k, n)};
-  R axy = rf<R>((double) n * (double) n), mm = rf<R>(1.0 / 6.0);
-  R muv = rf<R>(mu[(size_t) k * m + v]);
-  R four = rf<R>(4.0);
+  EA<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
+  R axy = sget<R>(axy_s), mm = sget<R>(sixth);
+  // the shift of each column, converted once per block
+  __shared__ R mu_s[32];
+  if (threadIdx.x < m) mu_s[threadIdx.x] = Real<R>::from(mu[(size_t) k * m + threadIdx.x]);
+  __syncthreads();
+  R muv = mu_s[v];
+  R four = rc<R>(4.0f);
   R s_r2 = Real<R>::zero(), s_v2 = Real<R>::zero(), s_ew = Real<R>::zero(), s_ev = Real<R>::zero(),
     s_ewi = Real<R>::zero();
   size_t nsite = (size_t) n * n;
   if (row < rows) {
-    for (size_t site = (size_t) blockIdx.x * rows + row; site < nsite; site += (size_t) gridDim.x * rows) {
-      int i = (int) (site % n), j = (int) (site / n);
+    for (int site = blockIdx.x * rows + row; site < (int) nsite; site += gridDim.x * rows) {
+      int i = site % n, j = site / n;
       cx<R> cc = curlc<R>(E, i, j);
       cx<R> cb = curlc<R>(E, i, j - 1);
       cx<R> cl = curlc<R>(E, i - 1, j);
@@ -152,6 +147,19 @@ struct GramArgs {
   double* partial;         // [K][chunks][nent][4]  (ga re, ga im, gm re, gm im)
   const float2* resid;     // optional c64 residual r_j of the high columns (see below)
   const double* theta;     // their Ritz values
+  Sc sixth;
+};
+
+// a high-precision value rounded to FP32 (the leading float of a pair)
+__device__ __forceinline__ cx<float> to_cf(cx<dd> v) { return mkc(v.re.hi, v.im.hi); }
+__device__ __forceinline__ cx<float> to_cf(cx<double> v) { return mkc((float) v.re, (float) v.im); }
+
+template <typename HI> struct KapHi;
+template <> struct KapHi<dd> {
+  __device__ static dd get(const mxk_kappa& k, size_t c) { return dd_make(k.dd[2 * c], k.dd[2 * c + 1]); }
+};
+template <> struct KapHi<double> {
+  __device__ static double get(const mxk_kappa& k, size_t c) { return k.d[c]; }
 };
 
 __device__ __forceinline__ cx<float> ld_any_f(int prec, const void* base, size_t off) {
@@ -176,8 +184,8 @@ __global__ void k_block_gram(GramArgs a, int mh) {
   float* kap_t = reinterpret_cast<float*>(kap_h + TS);                // TS
   cx<float>* rs = reinterpret_cast<cx<float>*>(kap_t + TS);          // TS*mh*2 (x, y of r)
   bool use_r = a.resid != nullptr;
-  Seam<float> sf = seam_of<float>(a.ph, k, n);
-  Seam<HI> sh = seam_of<HI>(a.ph, k, n);
+  Seam<float> sf = seam_load<float>(a.ph, a.K, k, n);
+  Seam<HI> sh = seam_load<HI>(a.ph, a.K, k, n);
   constexpr int MAXE = 5;   // ns <= 48 -> nent <= 1176 <= 5*256
   cx<float> acc_a[MAXE], acc_m[MAXE];
   cx<HI> hacc_a[MAXE], hacc_m[MAXE];
@@ -195,8 +203,8 @@ __global__ void k_block_gram(GramArgs a, int mh) {
       ei[t] = i; ej[t] = e - i * (i + 1) / 2;
     }
   }
-  HI mmh = Real<HI>::from(1.0 / 6.0), fourh = Real<HI>::from(4.0);
-  float mmf = 1.0f / 6.0f;
+  HI mmh = sget<HI>(a.sixth), fourh = rc<HI>(4.0f);
+  float mmf = a.sixth.hi;
   size_t nsite = (size_t) n * n;
   size_t per = (nsite + a.chunks - 1) / a.chunks;
   size_t s0 = (size_t) chunk * per, s1 = s0 + per < nsite ? s0 + per : nsite;
@@ -206,7 +214,7 @@ __global__ void k_block_gram(GramArgs a, int mh) {
       int ts = w / ns, col = w % ns;
       size_t site = base + ts;
       if (site >= s1) continue;
-      int i = (int) (site % n), j = (int) (site / n);
+      int i = (int) site % n, j = (int) site / n;
       int b = col / m, v = col % m;
       int prec = a.precs[b];
       size_t o0 = L.edge(k, 0, 0, 0, v);
@@ -226,11 +234,7 @@ __global__ void k_block_gram(GramArgs a, int mh) {
         }
         cx<HI>* hs = hi + ((size_t) ts * mh + col) * 5;
         hs[0] = c; hs[1] = x0; hs[2] = y0; hs[3] = mxv; hs[4] = myv;
-        ls[0] = mkc((float) Real<HI>::to_double(c.re), (float) Real<HI>::to_double(c.im));
-        ls[1] = mkc((float) Real<HI>::to_double(x0.re), (float) Real<HI>::to_double(x0.im));
-        ls[2] = mkc((float) Real<HI>::to_double(y0.re), (float) Real<HI>::to_double(y0.im));
-        ls[3] = mkc((float) Real<HI>::to_double(mxv.re), (float) Real<HI>::to_double(mxv.im));
-        ls[4] = mkc((float) Real<HI>::to_double(myv.re), (float) Real<HI>::to_double(myv.im));
+        ls[0] = to_cf(c); ls[1] = to_cf(x0); ls[2] = to_cf(y0); ls[3] = to_cf(mxv); ls[4] = to_cf(myv);
       } else {
         const void* pb = a.ptrs[b];
         auto X = [&](int p, int ii, int jj) {
@@ -252,7 +256,7 @@ __global__ void k_block_gram(GramArgs a, int mh) {
         int ts = w / mh, v = w % mh;
         size_t site = base + ts;
         if (site >= s1) continue;
-        int i = (int) (site % n), j = (int) (site / n);
+        int i = (int) site % n, j = (int) site / n;
         float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
         rs[((size_t) ts * mh + v) * 2] = mkc(rx.x, rx.y);
         rs[((size_t) ts * mh + v) * 2 + 1] = mkc(ry.x, ry.y);
@@ -261,7 +265,7 @@ __global__ void k_block_gram(GramArgs a, int mh) {
       size_t site = base + ts;
       if (site < s1) {
         kap_t[ts] = a.kap.f[site];
-        kap_h[ts] = Real<HI>::from(a.kap.d[site]);
+        kap_h[ts] = KapHi<HI>::get(a.kap, site);
       } else {
         kap_t[ts] = 0.0f;
         kap_h[ts] = Real<HI>::zero();
@@ -365,41 +369,82 @@ struct CombArgs {
   int precs[4];
   const void* ptrs[4];
   const double* coef;
+  const float4* cpair;     // coef as float-float pairs (re.hi, re.lo, im.hi, im.lo)
+};
+
+// coef -> float-float pairs, once per combine, so that the combine kernels
+// convert nothing in double
+__global__ void k_coef_pairs(const double* __restrict__ coef, float4* __restrict__ out, size_t len) {
+  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len) return;
+  dd r = dd_from_double(coef[2 * t]), i = dd_from_double(coef[2 * t + 1]);
+  out[t] = make_float4(r.hi, r.lo, i.hi, i.lo);
+}
+
+template <typename R> struct CoefGet {
+  __device__ static cx<R> get(const CombArgs& a, size_t at) {
+    float4 c = a.cpair[at];
+    return mkc(PairGet<R>::get(&c.x), PairGet<R>::get(&c.z));
+  }
+};
+template <> struct CoefGet<double> {
+  __device__ static cx<double> get(const CombArgs& a, size_t at) {
+    return mkc(a.coef[2 * at], a.coef[2 * at + 1]);
+  }
 };
 
 template <typename SO, typename RO>
 __global__ void k_block_combine(CombArgs a, SO* __restrict__ out) {
+  // block (m, rows): x = output column, y = entry (plane, site); grid.y = k.
+  // The coefficients are staged once per block in shared memory in the
+  // arithmetic of the block they multiply.
   int k = blockIdx.y;
   int m = a.m;
+  int nsrc = a.nb * m;
+  extern __shared__ float smc[];
+  cx<RO>* chi = reinterpret_cast<cx<RO>*>(smc);                    // nsrc * m
+  cx<float>* clo = reinterpret_cast<cx<float>*>(chi + nsrc * m);   // nsrc * m
+  size_t cbase = (size_t) k * a.ldc * m;
+  int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+  for (int e = tid; e < nsrc * m; e += nth) {
+    int i = e % nsrc, j = e / nsrc;
+    size_t at = cbase + (size_t) j * a.ldc + a.row0 + i;
+    int b = i / m;
+    if (a.precs[b] == MX_C64) {
+      float4 c = a.cpair[at];
+      clo[j * nsrc + i] = mkc(c.x, c.z);
+    } else {
+      chi[j * nsrc + i] = CoefGet<RO>::get(a, at);
+    }
+  }
+  __syncthreads();
   size_t per_k = (size_t) 2 * a.n * a.n * m;
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= per_k) return;
-  int j = (int) (t % m);
-  size_t ent = t / m;   // (plane, site)
-  size_t kbase = (size_t) k * per_k;
-  const double* C = a.coef + (size_t) k * 2 * a.ldc * m;
+  int j = threadIdx.x;
+  int ent = blockIdx.x * blockDim.y + threadIdx.y;
+  if (ent >= 2 * a.n * a.n) return;
+  size_t kbase = (size_t) k * per_k + (size_t) ent * m;
   cx<RO> acc_hi = czero<RO>();
   cx<float> acc_lo = czero<float>();
   for (int b = 0; b < a.nb; b++) {
     int prec = a.precs[b];
-    for (int i = 0; i < m; i++) {
-      size_t row = (size_t) a.row0 + (size_t) b * m + i;
-      double cr = C[2 * ((size_t) j * a.ldc + row)], ci = C[2 * ((size_t) j * a.ldc + row) + 1];
-      size_t off = kbase + ent * m + i;
-      if (prec == MX_C64) {
-        float2 s = ((const float2*) a.ptrs[b])[off];
-        acc_lo += mkc((float) cr, (float) ci) * mkc(s.x, s.y);
-      } else if (prec == MX_CDD) {
-        cx<RO> s = Store<cdd, RO>::ld((const cdd*) a.ptrs[b] + off);
-        acc_hi += cfrom<RO>(cr, ci) * s;
-      } else {
-        cx<RO> s = Store<double2, RO>::ld((const double2*) a.ptrs[b] + off);
-        acc_hi += cfrom<RO>(cr, ci) * s;
+    if (prec == MX_C64) {
+      const float2* src = (const float2*) a.ptrs[b] + kbase;
+      const cx<float>* cc = clo + j * nsrc + b * m;
+      for (int i = 0; i < m; i++) {
+        float2 v = src[i];
+        acc_lo += cc[i] * mkc(v.x, v.y);
+      }
+    } else {
+      const cx<RO>* cc = chi + j * nsrc + b * m;
+      for (int i = 0; i < m; i++) {
+        cx<RO> v = prec == MX_CDD ? Store<cdd, RO>::ld((const cdd*) a.ptrs[b] + kbase + i)
+                                  : Store<double2, RO>::ld((const double2*) a.ptrs[b] + kbase + i);
+        acc_hi += cc[i] * v;
       }
     }
   }
-  cx<RO> res = acc_hi + cfrom<RO>((double) acc_lo.re, (double) acc_lo.im);
-  Store<SO, RO>::st(out + kbase + ent * m + j, res);
+  cx<RO> res = acc_hi + mkc(Real<RO>::from_float(acc_lo.re), Real<RO>::from_float(acc_lo.im));
+  Store<SO, RO>::st(out + kbase + j, res);
 }
 
 // ------------------------------------------------------------------
@@ -415,7 +460,7 @@ __global__ void k_eps_sensitivity(int n, int m, int K, const double* __restrict_
   Lay L{n, m, K};
   double s = 0.0;
   for (int k = 0; k < K; k++) {
-    Seam<R> sm = seam_of<R>(ph, k, n);
+    Seam<R> sm = seam_load<R>(ph, K, k, n);
     for (int v = 0; v < m; v++) {
       double wv = w[(size_t) k * m + v];
       if (wv == 0.0) continue;
@@ -436,19 +481,22 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
   int rows = 256 / m;
   if (m > 32) return (int) cudaErrorInvalidValue;
   size_t nsite = (size_t) n * n;
-  unsigned G = (unsigned) ((nsite + (size_t) rows * 8 - 1) / ((size_t) rows * 8));
+  // about 32 sites per thread, so that the per-thread double reduction at
+  // the end stays small against the sweep
+  unsigned G = (unsigned) ((nsite + (size_t) rows * 32 - 1) / ((size_t) rows * 32));
   if (G < 1) G = 1;
   if (G > 4096) G = 4096;
   dim3 g(G, K), b(256);
   cudaStream_t st = (cudaStream_t) s;
+  Sc axy = make_sc((double) n * (double) n), sixth = make_sc(1.0 / 6.0);
   if (pe == MX_CDD && (pr == MX_C64 || !rout))
-    k_block_residual<cdd, float2, dd><<<g, b, 0, st>>>(n, m, K, ph, kapb<dd>(kap, n), mu, (const cdd*) e, (float2*) rout, stats);
+    k_block_residual<cdd, float2, dd><<<g, b, 0, st>>>(n, m, K, ph, kapb<dd>(kap, n), axy, sixth, mu, (const cdd*) e, (float2*) rout, stats);
   else if (pe == MX_C128 && (pr == MX_C128 || !rout))
-    k_block_residual<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), mu, (const double2*) e, (double2*) rout, stats);
+    k_block_residual<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), axy, sixth, mu, (const double2*) e, (double2*) rout, stats);
   else if (pe == MX_C128 && pr == MX_C64)
-    k_block_residual<double2, float2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), mu, (const double2*) e, (float2*) rout, stats);
+    k_block_residual<double2, float2, double><<<g, b, 0, st>>>(n, m, K, ph, kapb<double>(kap, n), axy, sixth, mu, (const double2*) e, (float2*) rout, stats);
   else if (pe == MX_C64 && (pr == MX_C64 || !rout))
-    k_block_residual<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, kapb<float>(kap, n), mu, (const float2*) e, (float2*) rout, stats);
+    k_block_residual<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, kapb<float>(kap, n), axy, sixth, mu, (const float2*) e, (float2*) rout, stats);
   else
     return (int) cudaErrorInvalidValue;
   MX_CHECK_LAUNCH();
@@ -477,6 +525,7 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
   a.ph = ph; a.kap = kap;
   a.resid = (const float2*) resid;
   a.theta = theta;
+  a.sixth = make_sc(1.0 / 6.0);
   int nent = a.ns * (a.ns + 1) / 2;
   a.chunks = gram_chunks(K, (size_t) n * n);
   size_t need = (size_t) K * a.chunks * nent * 4 * sizeof(double);
@@ -511,20 +560,29 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
 }
 
 extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, const void* const* ptrs,
-                                 const double* coef, int ldc, int row0, int pout, void* out, mx_stream s) {
+                                 const double* coef, int ldc, int row0, void* cwork, int pout, void* out,
+                                 mx_stream s) {
   if (nb < 1 || nb > 4) return (int) cudaErrorInvalidValue;
   CombArgs a;
   a.n = n; a.m = m; a.K = K; a.nb = nb; a.ldc = ldc; a.row0 = row0; a.coef = coef;
+  a.cpair = (const float4*) cwork;
+  size_t nc = (size_t) K * ldc * m;
+  k_coef_pairs<<<(unsigned) ((nc + 255) / 256), 256, 0, (cudaStream_t) s>>>(coef, (float4*) cwork, nc);
+  MX_CHECK_LAUNCH();
   for (int b = 0; b < 4; b++) {
     a.precs[b] = b < nb ? precs[b] : MX_C64;
     a.ptrs[b] = b < nb ? ptrs[b] : nullptr;
   }
-  size_t per_k = (size_t) 2 * n * n * m;
-  dim3 g((unsigned) ((per_k + 255) / 256), K), b(256);
+  unsigned rows = 256 / m;
+  dim3 g((unsigned) ((2 * (size_t) n * n + rows - 1) / rows), K), b(m, rows);
   cudaStream_t st = (cudaStream_t) s;
-  if (pout == MX_CDD) k_block_combine<cdd, dd><<<g, b, 0, st>>>(a, (cdd*) out);
-  else if (pout == MX_C128) k_block_combine<double2, double><<<g, b, 0, st>>>(a, (double2*) out);
-  else k_block_combine<float2, float><<<g, b, 0, st>>>(a, (float2*) out);
+  size_t ncoef = (size_t) nb * m * m;
+  if (pout == MX_CDD)
+    k_block_combine<cdd, dd><<<g, b, ncoef * (sizeof(cx<dd>) + sizeof(cx<float>)), st>>>(a, (cdd*) out);
+  else if (pout == MX_C128)
+    k_block_combine<double2, double><<<g, b, ncoef * (sizeof(cx<double>) + sizeof(cx<float>)), st>>>(a, (double2*) out);
+  else
+    k_block_combine<float2, float><<<g, b, ncoef * (sizeof(cx<float>) * 2), st>>>(a, (float2*) out);
   MX_CHECK_LAUNCH();
   return 0;
 }

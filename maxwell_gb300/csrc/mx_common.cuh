@@ -92,16 +92,19 @@ __host__ __device__ __forceinline__ double dd_to_double(dd a) { return (double) 
 // ------------------------------------------------------------------
 template <typename R> struct Real;
 template <> struct Real<float> {
+  __device__ static float from_float(float f) { return f; }
   __device__ static float from(double d) { return (float) d; }
   __device__ static double to_double(float f) { return (double) f; }
   __device__ static float zero() { return 0.0f; }
 };
 template <> struct Real<double> {
+  __device__ static double from_float(float f) { return (double) f; }
   __device__ static double from(double d) { return d; }
   __device__ static double to_double(double f) { return f; }
   __device__ static double zero() { return 0.0; }
 };
 template <> struct Real<dd> {
+  __device__ static dd from_float(float f) { return dd_make(f, 0.0f); }
   __device__ static dd from(double d) { return dd_from_double(d); }
   __device__ static double to_double(dd f) { return dd_to_double(f); }
   __device__ static dd zero() { return dd_make(0.0f, 0.0f); }
@@ -125,6 +128,36 @@ template <typename R> __device__ __forceinline__ cx<R> czero() { return mkc(Real
 template <typename R> __device__ __forceinline__ cx<R> cfrom(double re, double im) {
   return mkc(Real<R>::from(re), Real<R>::from(im));
 }
+// exactly representable literal constants (no double arithmetic at run time)
+template <typename R> __device__ __forceinline__ R rc(float f) { return Real<R>::from_float(f); }
+
+// ------------------------------------------------------------------
+// Scalars prepared on the host in all three arithmetics.  GB300 issues FP64
+// instructions at a small fraction of its FP32 rate, so the FP32 and
+// float-float kernels never compute or convert a constant in double: every
+// run-time scalar arrives as (double, float hi, float lo).
+// ------------------------------------------------------------------
+struct Sc {
+  double d;
+  float hi, lo;
+};
+inline Sc make_sc(double d) {
+  Sc s;
+  s.d = d;
+  s.hi = (float) d;
+  s.lo = (float) (d - (double) s.hi);
+  return s;
+}
+template <typename R> struct ScGet;
+template <> struct ScGet<float> { __device__ static float get(const Sc& s) { return s.hi; } };
+template <> struct ScGet<double> { __device__ static double get(const Sc& s) { return s.d; } };
+template <> struct ScGet<dd> { __device__ static dd get(const Sc& s) { return dd_make(s.hi, s.lo); } };
+template <typename R> __device__ __forceinline__ R sget(const Sc& s) { return ScGet<R>::get(s); }
+
+// a real number stored as a float-float pair (hi, lo) read in arithmetic R
+template <typename R> struct PairGet;
+template <> struct PairGet<float> { __device__ static float get(const float* p) { return p[0]; } };
+template <> struct PairGet<dd> { __device__ static dd get(const float* p) { return dd_make(p[0], p[1]); } };
 
 // ------------------------------------------------------------------
 // Storage <-> arithmetic conversions
@@ -214,7 +247,7 @@ struct Seam {
   // wrap (i,j) in place; returns the phase to multiply a fetched value by
   __device__ __forceinline__ bool wrap(int& i, int& j, cx<R>& ph) const {
     bool moved = false;
-    cx<R> p = cfrom<R>(1.0, 0.0);
+    cx<R> p = mkc(rc<R>(1.0f), Real<R>::zero());
     if (i < 0) { i += n; p = p * conjc(xf); moved = true; }
     else if (i >= n) { i -= n; p = p * xf; moved = true; }
     if (j < 0) { j += n; p = p * conjc(yf); moved = true; }
@@ -225,6 +258,34 @@ struct Seam {
 };
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Phase table of K k-points on the device: 4K doubles (re xf, im xf, re yf,
+// im yf of each k) followed by the same 4K numbers as 8K floats, each a
+// float-float pair (hi, lo).  FP32 kernels read the hi parts, float-float
+// kernels the pairs, FP64 kernels the doubles.
+template <typename R> struct SeamLoad {
+  __device__ static Seam<R> get(const double* ph, int K, int k, int n) {
+    const float* pf = reinterpret_cast<const float*>(ph + 4 * (size_t) K) + 8 * k;
+    Seam<R> s;
+    s.xf = mkc(PairGet<R>::get(pf + 0), PairGet<R>::get(pf + 2));
+    s.yf = mkc(PairGet<R>::get(pf + 4), PairGet<R>::get(pf + 6));
+    s.n = n;
+    return s;
+  }
+};
+template <> struct SeamLoad<double> {
+  __device__ static Seam<double> get(const double* ph, int K, int k, int n) {
+    Seam<double> s;
+    s.xf = mkc(ph[4 * k + 0], ph[4 * k + 1]);
+    s.yf = mkc(ph[4 * k + 2], ph[4 * k + 3]);
+    s.n = n;
+    return s;
+  }
+};
+template <typename R>
+__device__ __forceinline__ Seam<R> seam_load(const double* ph, int K, int k, int n) {
+  return SeamLoad<R>::get(ph, K, k, n);
+}
 
 // ------------------------------------------------------------------
 // Block reductions

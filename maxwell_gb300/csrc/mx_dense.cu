@@ -91,21 +91,20 @@ __global__ void k_hpd_inverse(int N, double* a, int* info) {
 // y_k = Ainv_k x_k on a level-0 block: the block of one k-point is a
 // row-major N x m matrix (dense row r at offset r*m)
 // ------------------------------------------------------------------
-template <typename S, typename R>
-__global__ void k_coarse_apply(int N, int m, const double* __restrict__ ainv, const S* __restrict__ x,
+// The inverse is read as MS (double2, or its float2 rounding for FP32 solves).
+template <typename S, typename R, typename MS>
+__global__ void k_coarse_apply(int N, int m, const MS* __restrict__ ainv, const S* __restrict__ x,
                                S* __restrict__ y) {
   int k = blockIdx.y;
-  const Z* Ai = reinterpret_cast<const Z*>(ainv) + (size_t) k * N * N;
+  const MS* Ai = ainv + (size_t) k * N * N;
   const S* xk = x + (size_t) k * N * m;
   S* yk = y + (size_t) k * N * m;
   size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t) N * m) return;
   int v = (int) (t % m), r = (int) (t / m);
   cx<R> acc = czero<R>();
-  for (int c = 0; c < N; c++) {
-    Z a = Ai[(size_t) c * N + r];
-    acc += cfrom<R>(a.re, a.im) * Store<S, R>::ld(xk + (size_t) c * m + v);
-  }
+  for (int c = 0; c < N; c++)
+    acc += Store<MS, R>::ld(Ai + (size_t) c * N + r) * Store<S, R>::ld(xk + (size_t) c * m + v);
   Store<S, R>::st(yk + (size_t) r * m + v, acc);
 }
 
@@ -135,16 +134,15 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
     if (i == j) AT(A, N, i, i).im = 0.0;
   }
   __syncthreads();
+  double fro = 0.0;
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) fro += zabs2(AT(A, N, e % N, e / N));
+  fro = sqrt(block_sum(fro, red));
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
-    double off = 0.0, dia = 0.0;
-    for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
-      int i = (int) (e % N), j = (int) (e / N);
-      double v = zabs2(AT(A, N, i, j));
-      if (i == j) dia += v; else off += v;
-    }
-    off = block_sum(off, red);
-    dia = block_sum(dia, red);
-    if (off <= 1e-30 * dia || off == 0.0) break;
+    // Rutishauser's test: a rotation is skipped when |a_pq| is negligible
+    // against sqrt(|a_pp a_qq|) or against the norm of the matrix (a block of
+    // equal or zero eigenvalues would otherwise be rotated forever); the
+    // iteration stops after a sweep without any rotation
+    double rotated = 0.0;
     for (int r = 0; r < Np - 1; r++) {
       for (int s = threadIdx.x; s < half; s += blockDim.x) {
         int a = s == 0 ? 0 : 1 + (s - 1 + r) % (Np - 1);
@@ -155,7 +153,9 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
         if (q < N) {
           Z apq = AT(A, N, p, q);
           double g = sqrt(zabs2(apq));
-          if (g > 0.0) {
+          double scale = sqrt(fabs(AT(A, N, p, p).re * AT(A, N, q, q).re));
+          if (g > 1e-16 * scale && g > 1e-15 * fro) {
+            rotated += 1.0;
             double app = AT(A, N, p, p).re, aqq = AT(A, N, q, q).re;
             double tau = (aqq - app) / (2.0 * g);
             double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
@@ -196,6 +196,7 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
       }
       __syncthreads();
     }
+    if (block_sum(rotated, red) == 0.0) break;
   }
   // eigenvalues, then sort ascending (selection sort by one thread on the
   // index permutation; N <= 256)
@@ -234,8 +235,8 @@ __global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
 // workspace per k: 4 * ns * ns complex doubles
 // ------------------------------------------------------------------
 __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, const double* __restrict__ gm,
-                                const int* __restrict__ sel, double drop, double* coef, double* theta,
-                                int* info, double* work) {
+                                const int* __restrict__ sel, double drop, double theta_min, double* coef,
+                                double* theta, int* info, double* work, int in_smem) {
   extern __shared__ double sm[];
   int k = blockIdx.x;
   int half = (ns + 1) / 2 + 1;
@@ -248,10 +249,19 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   int* cnt = kept + ns;                              // 2
   const double* GA = ga + (size_t) k * 2 * ns * ns;
   const double* GM = gm + (size_t) k * 2 * ns * ns;
-  double* W0 = work + (size_t) k * 8 * ns * ns;      // scaled Gram, then R
+  // work matrices: in shared memory for the Ritz systems (ns <= 48), in
+  // global memory for the coarse-grid eigenproblem
+  double* W0;
+  if (in_smem) {
+    uintptr_t p0 = reinterpret_cast<uintptr_t>(cnt + 2);
+    W0 = reinterpret_cast<double*>((p0 + 15) & ~(uintptr_t) 15);
+  } else {
+    W0 = work + (size_t) k * 8 * ns * ns;
+  }
   double* W1 = W0 + 2 * ns * ns;                     // T = D R^-1
   double* W2 = W1 + 2 * ns * ns;                     // G_A T, then projected A
   double* W3 = W2 + 2 * ns * ns;                     // Jacobi eigenvectors
+  double* GS = in_smem ? W3 + 2 * ns * ns : nullptr; // G_A on the selected columns
   if (threadIdx.x == 0) {
     int na = 0;
     for (int i = 0; i < ns; i++)
@@ -316,11 +326,21 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   }
   __syncthreads();
   // W3 <- G_A T  (na x r), then W2 <- T^H W3 (r x r)
+  if (GS) {
+    for (size_t e = threadIdx.x; e < (size_t) na * na; e += blockDim.x) {
+      int i = (int) (e % na), l = (int) (e / na);
+      AT(GS, na, i, l) = reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]];
+    }
+    __syncthreads();
+  }
   for (size_t e = threadIdx.x; e < (size_t) na * r; e += blockDim.x) {
     int i = (int) (e % na), c = (int) (e / na);
     Z s = zmk(0.0, 0.0);
-    for (int l = 0; l < na; l++)
-      s = zadd(s, zmul(reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]], AT(W1, na, l, c)));
+    if (GS)
+      for (int l = 0; l < na; l++) s = zadd(s, zmul(AT(GS, na, i, l), AT(W1, na, l, c)));
+    else
+      for (int l = 0; l < na; l++)
+        s = zadd(s, zmul(reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]], AT(W1, na, l, c)));
     AT(W3, na, i, c) = s;
   }
   __syncthreads();
@@ -332,7 +352,19 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   }
   __syncthreads();
   jacobi_cta(r, W2, W3, wv, shd, shi, 60);
-  // coefficients: rows idx[i] <- (T Y)[i, j], other rows zero
+  // Ritz values at or below theta_min are spurious (null-space) modes and
+  // are passed over, as exp_bloch2d.c:546-551 does for its coarse start
+  if (threadIdx.x == 0) {
+    int f = 0;
+    while (f < r && !(wv[f] > theta_min)) f++;
+    cnt[0] = f;
+  }
+  __syncthreads();
+  int first = cnt[0];
+  if (r - first < m) {
+    if (threadIdx.x == 0) info[k] = -1 - (r - first);
+    return;
+  }
   for (size_t e = threadIdx.x; e < (size_t) ns * m; e += blockDim.x) {
     int i = (int) (e % ns), j = (int) (e / ns);
     reinterpret_cast<Z*>(coef)[(size_t) k * ns * m + (size_t) j * ns + i] = zmk(0.0, 0.0);
@@ -341,10 +373,10 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   for (size_t e = threadIdx.x; e < (size_t) na * m; e += blockDim.x) {
     int i = (int) (e % na), j = (int) (e / na);
     Z s = zmk(0.0, 0.0);
-    for (int l = 0; l < r; l++) s = zadd(s, zmul(AT(W1, na, i, l), AT(W3, r, l, j)));
+    for (int l = 0; l < r; l++) s = zadd(s, zmul(AT(W1, na, i, l), AT(W3, r, l, first + j)));
     reinterpret_cast<Z*>(coef)[(size_t) k * ns * m + (size_t) j * ns + idx[i]] = s;
   }
-  for (int j = threadIdx.x; j < m; j += blockDim.x) theta[(size_t) k * m + j] = wv[j];
+  for (int j = threadIdx.x; j < m; j += blockDim.x) theta[(size_t) k * m + j] = wv[first + j];
   if (threadIdx.x == 0) info[k] = r;
 }
 
@@ -361,22 +393,23 @@ extern "C" int mxk_hpd_inverse(int N, int K, double* a, int* info, mx_stream s) 
   return 0;
 }
 
-template <typename S, typename R>
-static int L_coarse_apply(int N, int m, int K, const double* ainv, const void* x, void* y, cudaStream_t st) {
+template <typename S, typename R, typename MS>
+static int L_coarse_apply(int N, int m, int K, const void* ainv, const void* x, void* y, cudaStream_t st) {
   dim3 g((unsigned) (((size_t) N * m + 127) / 128), K);
-  k_coarse_apply<S, R><<<g, 128, 0, st>>>(N, m, ainv, (const S*) x, (S*) y);
+  k_coarse_apply<S, R, MS><<<g, 128, 0, st>>>(N, m, (const MS*) ainv, (const S*) x, (S*) y);
   MX_CHECK_LAUNCH();
   return 0;
 }
 
-extern "C" int mxk_coarse_apply(int N, int m, int K, const double* ainv, int prec, const void* x, void* y,
-                                int is_edge, int n, mx_stream s) {
-  (void) is_edge;
-  (void) n;
+extern "C" int mxk_coarse_apply(int N, int m, int K, const double* ainv, const void* ainv_c64, int prec,
+                                const void* x, void* y, mx_stream s) {
   cudaStream_t st = (cudaStream_t) s;
-  if (prec == MX_C64) return L_coarse_apply<float2, float>(N, m, K, ainv, x, y, st);
-  if (prec == MX_C128) return L_coarse_apply<double2, double>(N, m, K, ainv, x, y, st);
-  return L_coarse_apply<cdd, dd>(N, m, K, ainv, x, y, st);
+  if (prec == MX_C64) {
+    if (ainv_c64) return L_coarse_apply<float2, float, float2>(N, m, K, ainv_c64, x, y, st);
+    return L_coarse_apply<float2, float, double2>(N, m, K, ainv, x, y, st);
+  }
+  if (prec == MX_C128) return L_coarse_apply<double2, double, double2>(N, m, K, ainv, x, y, st);
+  return L_coarse_apply<cdd, dd, double2>(N, m, K, ainv, x, y, st);
 }
 
 extern "C" int mxk_heev(int N, int K, double* a, double* zwork, double* w, int* info, mx_stream s) {
@@ -386,10 +419,17 @@ extern "C" int mxk_heev(int N, int K, double* a, double* zwork, double* w, int* 
 }
 
 extern "C" int mxk_rayleigh_ritz(int ns, int m, int K, const double* ga, const double* gm, const int* sel,
-                                 double drop, double* coef, double* theta, int* info, double* work,
-                                 mx_stream s) {
+                                 double drop, double theta_min, double* coef, double* theta, int* info,
+                                 double* work, mx_stream s) {
   size_t smem = jacobi_smem(ns) + sizeof(int) * (2 * ns + 4) + sizeof(double) * (2 * ns + 2);
-  k_rayleigh_ritz<<<K, DT, smem, (cudaStream_t) s>>>(ns, m, ga, gm, sel, drop, coef, theta, info, work);
+  int in_smem = ns <= 48;
+  if (in_smem) {
+    smem += 16 + sizeof(double) * 2 * (size_t) ns * ns * 5;
+    cudaFuncSetAttribute(k_rayleigh_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  }
+  int threads = in_smem ? DT : 1024;
+  k_rayleigh_ritz<<<K, threads, smem, (cudaStream_t) s>>>(ns, m, ga, gm, sel, drop, theta_min, coef, theta, info,
+                                                         work, in_smem);
   MX_CHECK_LAUNCH();
   return 0;
 }

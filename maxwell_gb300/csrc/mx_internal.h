@@ -18,18 +18,34 @@ enum { MX_C64 = 0, MX_C128 = 1, MX_CDD = 2 };
 /* sizes of one complex entry */
 size_t mxk_elem_size(int prec);
 
+/* Phase table of K k-points (the `phases` argument of the kernels below):
+ * 4K doubles (re xf, im xf, re yf, im yf per k-point) followed by the same
+ * numbers as 8K floats in float-float pairs.  The caller writes the doubles
+ * into a host buffer of mxk_phase_bytes(K) bytes, calls mxk_phase_fill to
+ * derive the pairs, and copies the whole buffer to the device. */
+size_t mxk_phase_bytes(int K);
+void mxk_phase_fill(int K, double *host_table);
+
 /* per-level reciprocal permittivity in three precisions */
 typedef struct {
   const float *f;        /* n*n */
   const double *d;       /* n*n */
   const float *dd;       /* 2*n*n: (hi, lo) pairs */
+  const void *afw;       /* NULL or the AFW patch factors of mxk_afw_factors */
+  double afw_alpha, afw_beta;   /* the scalars those factors were made for */
 } mxk_kappa;
 
+/* Tabulate the FP32 factors of the AFW patch solves of one level (8 floats
+ * per vertex, n*n*32 bytes at out) for the operator alpha*A + beta*M; FP32
+ * sweeps with the same scalars read them instead of dividing per patch. */
+int mxk_afw_factors(int n, const float *kappa_f, double alpha, double beta, void *out, mx_stream s);
+
 /* ---- edge space ---- */
-/* y = cy*y + alpha*A x + beta_kv*M x; beta_kv (K*m doubles) or NULL -> beta */
+/* y = cy*(yin ? yin : y) + alpha*A x + beta_kv*M x; beta_kv (K*m doubles)
+ * or NULL -> beta; yin (precision prec_y) may be NULL; cy = 0 reads neither */
 int mxk_edge_apply(int n, int m, int K, const double *phases, mxk_kappa kap,
                    double alpha, double beta, const double *beta_kv, double cy,
-                   int prec_x, const void *x, int prec_y, void *y, mx_stream s);
+                   int prec_x, const void *x, int prec_y, const void *yin, void *y, mx_stream s);
 /* AFW line Gauss-Seidel sweep in the reference's row order; dir 0 forward,
  * 1 backward, 2 symmetric (forward then backward) */
 int mxk_edge_gs(int n, int m, int K, const double *phases, mxk_kappa kap,
@@ -41,8 +57,9 @@ int mxk_edge_restrict(int nc, int m, int K, const double *phases, double alpha,
                       int prec, const void *f, void *c, mx_stream s);
 
 /* ---- node space ---- */
+/* y = cy*(yin ? yin : y) + alpha*L x (Q1 Laplace); cy = 0 reads neither */
 int mxk_node_apply(int n, int m, int K, const double *phases, double alpha, double cy,
-                   int prec, const void *x, void *y, mx_stream s);
+                   int prec, const void *x, const void *yin, void *y, mx_stream s);
 int mxk_node_gs(int n, int m, int K, const double *phases, double alpha, int dir,
                 int prec, const void *b, void *x, mx_stream s);
 int mxk_node_prolong(int nc, int m, int K, const double *phases, double alpha,
@@ -66,8 +83,8 @@ int mxk_axpy(double are, double aim, int prec_x, const void *x, int prec_y, void
 int mxk_dot(size_t per, int m, int K, int prec_x, const void *x, int prec_y, const void *y,
             double *out, mx_stream s);
 /* Remove the mean of each plane of every (k, vector) (center_edge2d at k = 0);
- * only applied to k-points whose flag is set. */
-int mxk_center(int n, int m, int K, const int *gamma_flag, int prec, void *x, mx_stream s);
+ * only applied to k-points whose flag is set.  acc: 4*K*m doubles of scratch. */
+int mxk_center(int n, int m, int K, const int *gamma_flag, int prec, void *x, double *acc, mx_stream s);
 
 /* ---- coarse dense matrices (one per k, column-major, complex double) ---- */
 /* A = alpha*A + beta*M on the 2n^2 edges of level 0 */
@@ -80,9 +97,10 @@ int mxk_dense_node(int n, int K, const double *phases, int fixnull, double *a, m
 /* in-place inverse of K Hermitian positive definite N x N matrices; info[k] != 0 on breakdown */
 int mxk_hpd_inverse(int N, int K, double *a, int *info, mx_stream s);
 /* y[k] = A[k] x[k] for K blocks, x,y with m columns in the batched layout of a
- * level-0 edge (N = 2n^2) or node (N = n^2) block */
-int mxk_coarse_apply(int N, int m, int K, const double *ainv, int prec, const void *x,
-                     void *y, int is_edge, int n, mx_stream s);
+ * level-0 edge (N = 2n^2) or node (N = n^2) block; ainv_c64 (may be NULL) is
+ * the c64 rounding of ainv that c64 solves read instead */
+int mxk_coarse_apply(int N, int m, int K, const double *ainv, const void *ainv_c64, int prec,
+                     const void *x, void *y, mx_stream s);
 /* Hermitian eigendecomposition by parallel cyclic Jacobi: a (lower triangle
  * used) is overwritten with eigenvectors, w with ascending eigenvalues;
  * zwork: K*N*N complex doubles of scratch */
@@ -91,9 +109,10 @@ int mxk_heev(int N, int K, double *a, double *zwork, double *w, int *info, mx_st
  * column i), unit-diagonal scaling, Cholesky with column dropping
  * (pivot^2 <= drop), Jacobi on the projected A.  Outputs the lowest m Ritz
  * values and the ns x m coefficients (zero rows for dropped columns). */
-/* work: 8*ns*ns doubles per k */
+/* Ritz values <= theta_min are skipped (spurious null-space modes);
+ * work: 8*ns*ns doubles per k */
 int mxk_rayleigh_ritz(int ns, int m, int K, const double *ga, const double *gm,
-                      const int *sel, double drop, double *coef, double *theta,
+                      const int *sel, double drop, double theta_min, double *coef, double *theta,
                       int *info, double *work, mx_stream s);
 
 /* ---- block (eigenvector) kernels ---- */
@@ -114,10 +133,11 @@ int mxk_block_gram(int n, int m, int K, const double *phases, mxk_kappa kap, int
                    const int *precs, const void *const *ptrs, const void *resid,
                    const double *theta, double *ga, double *gm,
                    double *scratch, size_t scratch_bytes, mx_stream s);
-/* out_j = sum_i coef(i,j) S_i for the blocks listed; coef is ns x m per k,
- * only rows [row0, row0 + nb*m) are used */
+/* out_j = sum_i coef(i,j) S_i for the blocks listed; coef is ldc x m per k,
+ * only rows [row0, row0 + nb*m) are used; cwork: K*ldc*m*16 bytes that take
+ * the coefficients as float-float pairs */
 int mxk_block_combine(int n, int m, int K, int nb, const int *precs, const void *const *ptrs,
-                      const double *coef, int ldc, int row0, int prec_out, void *out,
+                      const double *coef, int ldc, int row0, void *cwork, int prec_out, void *out,
                       mx_stream s);
 /* per-cell eigenvalue sensitivity: grad[c] = -n^2 kappa_c^2 sum_{k,v} w[k*m+v] |curl_c e|^2 */
 int mxk_eps_sensitivity(int n, int m, int K, const double *phases, const double *kappa,

@@ -17,6 +17,7 @@
  * inverses.  Residuals are r_i = (A+M) e_i - mu_i M e_i with, as the
  * stopping rule, either the reference's absolute norm or ||r_i|| / (mu_i ||M e_i||).
  */
+#define _POSIX_C_SOURCE 200809L
 #include "maxwell_gb300.h"
 #include "mx_internal.h"
 
@@ -29,6 +30,19 @@
 #define MAXL 16
 #define NSTAT 5
 
+#include <time.h>
+static double now_s(void)
+{
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+/* GPU time per phase of the block steps at the finest level (CUDA events,
+ * read once per step), reported with MXG_TIMING set */
+enum { PH_PREC, PH_LIFTX, PH_GRAM, PH_RR, PH_COMB, PH_LIFTE, PH_RESID, PH_N };
+static const char *ph_name[PH_N] = {"precondition", "lift X", "gram", "rayleigh-ritz", "combine", "lift E",
+                                    "residual"};
+
 struct mxg_solver {
   mxg_solve_opts o;
   int n0, L, m, K, pe, pg;
@@ -37,15 +51,19 @@ struct mxg_solver {
   int n[MAXL];
   double *kd[MAXL];
   float *kf[MAXL], *kdd[MAXL];
-  double *ph;                        /* K*4 */
+  void *kafw[MAXL];                  /* AFW patch factors (alpha = beta = 1) */
+  double *ph;                        /* phase table (mxk_phase_bytes) */
   int *gamma;                        /* K flags */
   void *b[MAXL], *x[MAXL], *d[MAXL];
   void *bg[MAXL], *xg[MAXL], *dg[MAXL];
   double *ae_inv, *an_inv;
+  void *ae_inv_f, *an_inv_f;         /* their c64 roundings (FP32 solves) */
   void *E, *En, *P, *Pn, *Eprev;
   double *ga, *gm, *coef, *theta, *rwork, *gscratch, *mu, *stats;
   size_t gscratch_bytes;
   int *sel, *info;
+  double *cacc;                      /* 4*K*m: plane means of center */
+  void *combw;                       /* K*ns*m*16: combine coefficients */
   double *cA, *cM, *ccoef, *ctheta, *cwork;   /* coarse eigenproblem */
   int *cinfo;
   /* host */
@@ -54,6 +72,15 @@ struct mxg_solver {
   int have_prev, K_prev;
   double last_ms;
   long launches;
+  /* CUDA-event timing of the finest-level AFW sweeps (the dominant kernel) */
+  int timing;
+  cudaEvent_t tev[PH_N + 1];
+  double tph[PH_N];
+  int prof;
+  cudaEvent_t *pev;
+  int npev, maxpev;
+  double prof_ms;
+  long prof_count;
 };
 
 #define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
@@ -63,6 +90,7 @@ static mxk_kappa kap(const mxg_solver *s, int l)
 {
   mxk_kappa k;
   k.f = s->kf[l]; k.d = s->kd[l]; k.dd = s->kdd[l];
+  k.afw = s->kafw[l]; k.afw_alpha = 1.0; k.afw_beta = 1.0;
   return k;
 }
 
@@ -79,16 +107,23 @@ void mxg_solver_free(mxg_solver *s)
   int l;
   if(!s) return;
   for(l = 0; l <= s->L; l++) {
-    cudaFree(s->kd[l]); cudaFree(s->kf[l]); cudaFree(s->kdd[l]);
+    cudaFree(s->kd[l]); cudaFree(s->kf[l]); cudaFree(s->kdd[l]); cudaFree(s->kafw[l]);
     cudaFree(s->b[l]); cudaFree(s->x[l]); cudaFree(s->d[l]);
     cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
   }
-  cudaFree(s->ph); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv);
+  cudaFree(s->ph); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv); cudaFree(s->ae_inv_f); cudaFree(s->an_inv_f);
   cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn); cudaFree(s->Eprev);
   cudaFree(s->ga); cudaFree(s->gm); cudaFree(s->coef); cudaFree(s->theta); cudaFree(s->rwork);
   cudaFree(s->gscratch); cudaFree(s->mu); cudaFree(s->stats); cudaFree(s->sel); cudaFree(s->info);
   cudaFree(s->cA); cudaFree(s->cM); cudaFree(s->ccoef); cudaFree(s->ctheta); cudaFree(s->cwork);
   cudaFree(s->cinfo);
+  cudaFree(s->cacc);
+  cudaFree(s->combw);
+  if(s->pev) {
+    int q;
+    for(q = 0; q < s->maxpev; q++) cudaEventDestroy(s->pev[q]);
+    free(s->pev);
+  }
   if(s->st) cudaStreamDestroy(s->st);
   if(s->ev0) cudaEventDestroy(s->ev0);
   if(s->ev1) cudaEventDestroy(s->ev1);
@@ -142,10 +177,11 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
       p[2 * q + 1] = (float) (kk[l][q] - (double) p[2 * q]);
     }
     if(dalloc((void **) &s->kd[l], sizeof(double) * nn) || dalloc((void **) &s->kf[l], sizeof(float) * nn)
-       || dalloc((void **) &s->kdd[l], sizeof(float) * 2 * nn)
+       || dalloc((void **) &s->kdd[l], sizeof(float) * 2 * nn) || dalloc(&s->kafw[l], 32 * nn)
        || cudaMemcpy(s->kd[l], kk[l], sizeof(double) * nn, cudaMemcpyHostToDevice)
        || cudaMemcpy(s->kf[l], f, sizeof(float) * nn, cudaMemcpyHostToDevice)
-       || cudaMemcpy(s->kdd[l], p, sizeof(float) * 2 * nn, cudaMemcpyHostToDevice)) {
+       || cudaMemcpy(s->kdd[l], p, sizeof(float) * 2 * nn, cudaMemcpyHostToDevice)
+       || mxk_afw_factors(n, s->kf[l], 1.0, 1.0, s->kafw[l], s->st) || cudaStreamSynchronize(s->st)) {
       free(f); free(p);
       for(; l <= o->L; l++) free(kk[l]);
       goto fail;
@@ -158,9 +194,11 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
        || dalloc(&s->bg[l], nlen(s, l) * es_g) || dalloc(&s->xg[l], nlen(s, l) * es_g)
        || dalloc(&s->dg[l], nlen(s, l) * es_g))
       goto fail;
-  if(dalloc((void **) &s->ph, sizeof(double) * 4 * K) || dalloc((void **) &s->gamma, sizeof(int) * K)
+  if(dalloc((void **) &s->ph, mxk_phase_bytes(K)) || dalloc((void **) &s->gamma, sizeof(int) * K)
      || dalloc((void **) &s->ae_inv, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->an_inv, sizeof(double) * 2 * (size_t) N0n * N0n * K)
+     || dalloc(&s->ae_inv_f, sizeof(float) * 2 * (size_t) N0e * N0e * K)
+     || dalloc(&s->an_inv_f, sizeof(float) * 2 * (size_t) N0n * N0n * K)
      || dalloc(&s->E, elen(s, o->L) * es_e) || dalloc(&s->En, elen(s, o->L) * es_e)
      || dalloc(&s->Eprev, elen(s, o->L) * es_e)
      || dalloc(&s->P, elen(s, o->L) * es_g) || dalloc(&s->Pn, elen(s, o->L) * es_g)
@@ -174,12 +212,14 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
      || dalloc((void **) &s->ccoef, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->ctheta, sizeof(double) * (size_t) N0e * K)
      || dalloc((void **) &s->cwork, sizeof(double) * 8 * (size_t) N0e * N0e * K)
-     || dalloc((void **) &s->cinfo, sizeof(int) * K))
+     || dalloc((void **) &s->cinfo, sizeof(int) * K)
+     || dalloc((void **) &s->cacc, sizeof(double) * 4 * K * m)
+     || dalloc(&s->combw, (size_t) 16 * ns * m * K))
     goto fail;
   s->gscratch_bytes = (size_t) K * 256 * (ns * (ns + 1) / 2) * 4 * sizeof(double);
   if(s->gscratch_bytes > ((size_t) 1 << 30)) s->gscratch_bytes = (size_t) 1 << 30;
   if(dalloc((void **) &s->gscratch, s->gscratch_bytes)) goto fail;
-  s->h_ph = malloc(sizeof(double) * 4 * K);
+  s->h_ph = malloc(mxk_phase_bytes(K));
   s->h_stats = malloc(sizeof(double) * NSTAT * m * K);
   s->h_mu = malloc(sizeof(double) * m * K);
   s->h_res = malloc(sizeof(double) * m * K);
@@ -188,6 +228,11 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   s->h_info = malloc(sizeof(int) * K);
   s->h_conv = malloc(sizeof(int) * K);
   s->h_steps = malloc(sizeof(int) * K);
+  s->timing = getenv("MXG_TIMING") != 0;
+  if(s->timing) {
+    int q;
+    for(q = 0; q <= PH_N; q++) cudaEventCreate(&s->tev[q]);
+  }
   return s;
 fail:
   mxg_solver_free(s);
@@ -205,7 +250,8 @@ static int set_bloch(mxg_solver *s, int K, const mxg_field *xf, const mxg_field 
     s->h_ph[4 * k + 2] = creal(yf[q]); s->h_ph[4 * k + 3] = cimag(yf[q]);
     g[k] = xf[q] == 1.0 && yf[q] == 1.0;
   }
-  e = (int) cudaMemcpyAsync(s->ph, s->h_ph, sizeof(double) * 4 * s->K, cudaMemcpyHostToDevice, s->st);
+  mxk_phase_fill(s->K, s->h_ph);
+  e = (int) cudaMemcpyAsync(s->ph, s->h_ph, mxk_phase_bytes(s->K), cudaMemcpyHostToDevice, s->st);
   if(!e) e = (int) cudaMemcpyAsync(s->gamma, g, sizeof(int) * s->K, cudaMemcpyHostToDevice, s->st);
   if(!e) e = (int) cudaStreamSynchronize(s->st);
   free(g);
@@ -229,7 +275,37 @@ static int factor_coarse(mxg_solver *s)
   TRY((int) cudaStreamSynchronize(s->st));
   for(k = 0; k < s->K; k++)
     if(s->h_info[k]) return MXG_ECONV;
+  L_(mxk_convert(MX_C128, s->ae_inv, MX_C64, s->ae_inv_f, (size_t) N0e * N0e * s->K, s->st));
+  L_(mxk_convert(MX_C128, s->an_inv, MX_C64, s->an_inv_f, (size_t) N0n * N0n * s->K, s->st));
   return 0;
+}
+
+static void prof_flush(mxg_solver *s)
+{
+  int q;
+  cudaEventSynchronize(s->pev[s->npev > 0 ? s->npev - 1 : 0]);
+  for(q = 0; q + 1 < s->npev; q += 2) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, s->pev[q], s->pev[q + 1]);
+    s->prof_ms += ms;
+    s->prof_count++;
+  }
+  s->npev = 0;
+}
+
+/* one AFW sweep; the finest level's sweeps are timed when profiling is on */
+static int edge_gs(mxg_solver *s, int l, int dir)
+{
+  int timed = s->prof && l == s->L;
+  int e;
+  if(timed) {
+    if(s->npev + 2 > s->maxpev) prof_flush(s);
+    cudaEventRecord(s->pev[s->npev++], s->st);
+  }
+  e = mxk_edge_gs(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
+  s->launches += 2 * (dir == 2 ? 2 : 1);
+  if(timed) cudaEventRecord(s->pev[s->npev++], s->st);
+  return e;
 }
 
 /* vcycle_edge2d (edge2d.c:5707-5754) on b[top], x[top] with the coarse inverse */
@@ -239,19 +315,18 @@ static int vcycle_e(mxg_solver *s, int top)
   for(l = top; l > 0; l--) {
     int n = s->n[l];
     for(i = 0; i < nu; i++)
-      L_(mxk_edge_gs(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 0, pg, s->b[l], s->x[l], s->st));
-    L_(mxk_convert(pg, s->b[l], pg, s->d[l], elen(s, l), s->st));
-    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->d[l], s->st));
+      TRY(edge_gs(s, l, 0));
+    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
     L_(mxk_zero(pg, s->b[l - 1], elen(s, l - 1), s->st));
     L_(mxk_edge_restrict(n / 2, m, K, s->ph, 1.0, pg, s->d[l], s->b[l - 1], s->st));
     L_(mxk_zero(pg, s->x[l - 1], elen(s, l - 1), s->st));
   }
-  L_(mxk_coarse_apply(2 * s->n0 * s->n0, m, K, s->ae_inv, pg, s->b[0], s->x[0], 1, s->n0, s->st));
+  L_(mxk_coarse_apply(2 * s->n0 * s->n0, m, K, s->ae_inv, s->ae_inv_f, pg, s->b[0], s->x[0], s->st));
   for(l = 1; l <= top; l++) {
     int n = s->n[l];
     L_(mxk_edge_prolong(n / 2, m, K, s->ph, 1.0, pg, s->x[l - 1], s->x[l], s->st));
     for(i = 0; i < nu; i++)
-      L_(mxk_edge_gs(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 1, pg, s->b[l], s->x[l], s->st));
+      TRY(edge_gs(s, l, 1));
   }
   return 0;
 }
@@ -262,20 +337,23 @@ static int vcycle_n(mxg_solver *s, int top)
   int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
   for(l = top; l > 0; l--) {
     int n = s->n[l];
-    for(i = 0; i < nu; i++)
+    for(i = 0; i < nu; i++) {
       L_(mxk_node_gs(n, m, K, s->ph, 1.0, 0, pg, s->bg[l], s->xg[l], s->st));
-    L_(mxk_convert(pg, s->bg[l], pg, s->dg[l], nlen(s, l), s->st));
-    L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->dg[l], s->st));
+      s->launches += 3;   /* four row groups */
+    }
+    L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->bg[l], s->dg[l], s->st));
     L_(mxk_zero(pg, s->bg[l - 1], nlen(s, l - 1), s->st));
     L_(mxk_node_restrict(n / 2, m, K, s->ph, 1.0, pg, s->dg[l], s->bg[l - 1], s->st));
     L_(mxk_zero(pg, s->xg[l - 1], nlen(s, l - 1), s->st));
   }
-  L_(mxk_coarse_apply(s->n0 * s->n0, m, K, s->an_inv, pg, s->bg[0], s->xg[0], 0, s->n0, s->st));
+  L_(mxk_coarse_apply(s->n0 * s->n0, m, K, s->an_inv, s->an_inv_f, pg, s->bg[0], s->xg[0], s->st));
   for(l = 1; l <= top; l++) {
     int n = s->n[l];
     L_(mxk_node_prolong(n / 2, m, K, s->ph, 1.0, pg, s->xg[l - 1], s->xg[l], s->st));
-    for(i = 0; i < nu; i++)
+    for(i = 0; i < nu; i++) {
       L_(mxk_node_gs(n, m, K, s->ph, 1.0, 1, pg, s->bg[l], s->xg[l], s->st));
+      s->launches += 3;
+    }
   }
   return 0;
 }
@@ -348,12 +426,14 @@ static void swapp(void **a, void **b)
 
 /* Rayleigh-Ritz on the nb blocks (precisions pr, pointers pp) -> coef, theta
  * with soft locking of converged columns; writes the new E (and P) */
-static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop)
+static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop,
+                double theta_min)
 {
   int m = s->m, K = s->K, ns = nb * m, k, i, j;
   /* the residual of E sits in b[l] (written by residual()) with the Ritz
    * values mu; the mixed solver forms the E-to-search-block entries from it */
   const void *rr = (s->pe == MX_CDD && nb > 1) ? s->b[l] : 0;
+  int tm = s->timing && l == s->L && nb > 1;
   L_(mxk_block_gram(s->n[l], m, K, s->ph, kap(s, l), nb, pr, pp, rr, s->mu, s->ga, s->gm, s->gscratch,
                     s->gscratch_bytes, s->st));
   for(k = 0; k < K; k++)
@@ -361,15 +441,18 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
       for(i = 0; i < m; i++)
         s->h_sel[k * ns + j * m + i] = j == 0 || !(s->h_res[k * m + i] <= s->o.tol);
   TRY((int) cudaMemcpyAsync(s->sel, s->h_sel, sizeof(int) * ns * K, cudaMemcpyHostToDevice, s->st));
-  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop, s->coef, s->theta, s->info, s->rwork, s->st));
+  if(tm) cudaEventRecord(s->tev[PH_RR], s->st);
+  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop, theta_min, s->coef, s->theta, s->info, s->rwork,
+                       s->st));
   TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * K, cudaMemcpyDeviceToHost, s->st));
   TRY((int) cudaMemcpyAsync(s->h_mu, s->theta, sizeof(double) * m * K, cudaMemcpyDeviceToHost, s->st));
   TRY((int) cudaStreamSynchronize(s->st));
   for(k = 0; k < K; k++)
     if(s->h_info[k] < m) return MXG_ECONV;
+  if(tm) cudaEventRecord(s->tev[PH_COMB], s->st);
   if(with_p)
-    L_(mxk_block_combine(s->n[l], m, K, nb - 1, pr + 1, pp + 1, s->coef, ns, m, s->pg, s->Pn, s->st));
-  L_(mxk_block_combine(s->n[l], m, K, nb, pr, pp, s->coef, ns, 0, s->pe, s->En, s->st));
+    L_(mxk_block_combine(s->n[l], m, K, nb - 1, pr + 1, pp + 1, s->coef, ns, m, s->combw, s->pg, s->Pn, s->st));
+  L_(mxk_block_combine(s->n[l], m, K, nb, pr, pp, s->coef, ns, 0, s->combw, s->pe, s->En, s->st));
   swapp(&s->E, &s->En);
   if(with_p) swapp(&s->P, &s->Pn);
   return upload_mu(s);
@@ -393,27 +476,35 @@ static int block_step(mxg_solver *s, int l, int *have_p)
     const void *pp[1];
     TRY(precondition(s, l));
     L_(mxk_axpy(-1.0, 0.0, s->pg, s->x[l], s->pe, s->E, len, s->st));
-    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->st));
+    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->cacc, s->st));
     TRY(lift(s, l, s->pe, s->E));
     pr[0] = s->pe; pp[0] = s->E;
-    return ritz(s, l, 1, pr, pp, 0, 1e-14);
+    return ritz(s, l, 1, pr, pp, 0, 1e-14, -1e300);
   }
   else {
     int pr[3], nb;
     const void *pp[3];
+    int tm = s->timing && l == s->L;
+    if(tm) cudaEventRecord(s->tev[PH_PREC], s->st);
     TRY(precondition(s, l));
-    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pg, s->x[l], s->st));
+    if(tm) cudaEventRecord(s->tev[PH_LIFTX], s->st);
+    if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pg, s->x[l], s->cacc, s->st));
     TRY(lift(s, l, s->pg, s->x[l]));
+    if(tm) cudaEventRecord(s->tev[PH_GRAM], s->st);
     pr[0] = s->pe; pp[0] = s->E;
     pr[1] = s->pg; pp[1] = s->x[l];
     pr[2] = s->pg; pp[2] = s->P;
     nb = *have_p ? 3 : 2;
-    TRY(ritz(s, l, nb, pr, pp, 1, drop_tol(s)));
+    /* mu = 1 + lambda: pairs with lambda <= 1e-7 are gradient (null-space)
+     * modes that the search directions' rounding can expose */
+    TRY(ritz(s, l, nb, pr, pp, 1, drop_tol(s), 1.0 + 1e-7));
+    if(tm) cudaEventRecord(s->tev[PH_LIFTE], s->st);
     *have_p = 1;
     if(s->o.lift_e) {
-      if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->st));
+      if(s->o.center) L_(mxk_center(s->n[l], m, s->K, s->gamma, s->pe, s->E, s->cacc, s->st));
       TRY(lift(s, l, s->pe, s->E));
     }
+    if(tm) cudaEventRecord(s->tev[PH_RESID], s->st);
     return 0;
   }
 }
@@ -433,6 +524,18 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
     if(all) break;
     TRY(block_step(s, l, &have_p));
     TRY(residual(s, l, 1));
+    if(s->timing && l == s->L && s->o.method == 1) {
+      int q;
+      cudaEventRecord(s->tev[PH_N], s->st);
+      cudaEventSynchronize(s->tev[PH_N]);
+      for(q = 0; q < PH_N; q++) {
+        float ms = 0.0f;
+        cudaError_t er = cudaEventElapsedTime(&ms, s->tev[q], s->tev[q + 1]);
+        if(er != cudaSuccess) fprintf(stderr, "timing event %d: %s\n", q, cudaGetErrorString(er));
+        s->tph[q] += ms;
+      }
+      cudaGetLastError();
+    }
     if(getenv("MXG_DEBUG")) {
       int i;
       fprintf(stderr, "level %d step %d rank %d:", l, step, s->h_info[0]);
@@ -455,7 +558,7 @@ static int cold_start(mxg_solver *s, int K_active)
   int e = 0;
   L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 1.0, 0.0, s->cA, s->st));
   L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 0.0, 1.0, s->cM, s->st));
-  L_(mxk_rayleigh_ritz(N, N, K, s->cA, s->cM, 0, 1e-14, s->ccoef, s->ctheta, s->cinfo, s->cwork, s->st));
+  L_(mxk_rayleigh_ritz(N, N, K, s->cA, s->cM, 0, 1e-14, -1e300, s->ccoef, s->ctheta, s->cinfo, s->cwork, s->st));
   e = (int) cudaMemcpyAsync(th, s->ctheta, sizeof(double) * N * K, cudaMemcpyDeviceToHost, s->st);
   if(!e) e = (int) cudaMemcpyAsync(cf, s->ccoef, sizeof(double) * 2 * (size_t) N * N * K, cudaMemcpyDeviceToHost, s->st);
   if(!e) e = (int) cudaStreamSynchronize(s->st);
@@ -515,13 +618,16 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
   float ms;
   double total = 0.0;
   s->launches = 0;
+  s->have_prev = 0;   /* every call starts cold; later waves of this call start warm */
   for(w = 0; w * K < nk; w++) {
     int k0 = w * K, Ka = nk - k0 < K ? nk - k0 : K;
     TRY(set_bloch(s, Ka, xf + k0, yf + k0));
     TRY((int) cudaEventRecord(s->ev0, s->st));
     TRY(factor_coarse(s));
     if(!s->have_prev || s->K_prev != K) {
+      double tc = now_s();
       TRY(cold_start(s, Ka));
+      if(s->timing) fprintf(stderr, "wave %d: cold start incl. finest-level steps %.3f s\n", w, now_s() - tc);
     }
     else {
       /* warm start from the k-point one wave earlier (extrapolation 'n') */
@@ -547,6 +653,14 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
     s->K_prev = K;
   }
   s->last_ms = total;
+  if(s->timing) {
+    int q;
+    fprintf(stderr, "finest-level GPU time per phase:");
+    for(q = 0; q < PH_N; q++) {
+      fprintf(stderr, " %s %.3f s%s", ph_name[q], s->tph[q] / 1e3, q + 1 < PH_N ? "," : "\n");
+      s->tph[q] = 0.0;
+    }
+  }
   return (int) cudaStreamSynchronize(s->st);
 }
 
@@ -579,6 +693,36 @@ int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches)
 {
   if(ms) *ms = s->last_ms;
   if(launches) *launches = s->launches;
+  return 0;
+}
+
+int mxg_solver_profile(mxg_solver *s, int enable)
+{
+  if(enable && !s->pev) {
+    int q;
+    s->maxpev = 4096;
+    s->pev = malloc(sizeof(cudaEvent_t) * s->maxpev);
+    for(q = 0; q < s->maxpev; q++)
+      if(cudaEventCreate(&s->pev[q])) return MXG_ENOMEM;
+  }
+  s->prof = enable;
+  s->npev = 0;
+  s->prof_ms = 0.0;
+  s->prof_count = 0;
+  return 0;
+}
+
+int mxg_solver_kernel_time(mxg_solver *s, double *ms, long *count, double *bytes_per_sweep)
+{
+  /* algorithmic bytes of one forward or backward AFW sweep at the finest
+   * level (both row phases): read x, b and kappa once, write x once:
+   * 3 * 2n^2 complex entries per vector plus n^2 kappa values */
+  size_t n = (size_t) s->n[s->L];
+  if(s->prof && s->npev) prof_flush(s);
+  if(ms) *ms = s->prof_ms;
+  if(count) *count = s->prof_count;
+  if(bytes_per_sweep)
+    *bytes_per_sweep = (double) s->K * s->m * 3.0 * 2.0 * n * n * mxk_elem_size(s->pg) + (double) n * n * 4.0;
   return 0;
 }
 

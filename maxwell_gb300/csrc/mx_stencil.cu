@@ -21,19 +21,18 @@ namespace {
 
 constexpr int TPB = 256;
 
+// launch geometry of the site kernels: block (m, 256/m), grid (sites/rows, K)
+inline dim3 blk2(int m) { return dim3(m, 256 / m); }
+inline dim3 grd2(size_t sites, int m, int K) {
+  unsigned rows = 256 / m;
+  return dim3((unsigned) ((sites + rows - 1) / rows), K);
+}
+
 inline unsigned nblocks(size_t work, int tpb = TPB) {
   size_t b = (work + tpb - 1) / tpb;
   return (unsigned) (b > 0x7fffffff ? 0x7fffffff : b);
 }
 
-template <typename R>
-__device__ __forceinline__ Seam<R> load_seam(const double* ph, int k, int n) {
-  Seam<R> s;
-  s.xf = cfrom<R>(ph[4 * k + 0], ph[4 * k + 1]);
-  s.yf = cfrom<R>(ph[4 * k + 2], ph[4 * k + 3]);
-  s.n = n;
-  return s;
-}
 
 // kappa of cell (i,j) with periodic wrap, in arithmetic R
 template <typename R> struct Kap;
@@ -84,7 +83,6 @@ struct NAcc {
   }
 };
 
-template <typename R> __device__ __forceinline__ R rfrom(double d) { return Real<R>::from(d); }
 
 // curl of cell (i,j): bottom - top - left + right
 template <typename R, typename A>
@@ -96,59 +94,58 @@ __device__ __forceinline__ cx<R> curl(const A& E, int i, int j) {
 template <typename R, typename A>
 __device__ __forceinline__ cx<R> kx_x(const A& E, const Kap<R>& kap, R axy, R mm, int i, int j) {
   cx<R> c0 = E(0, i, j);
-  cx<R> mass = scal(mm, scal(rfrom<R>(4.0), c0) + E(0, i, j + 1) + E(0, i, j - 1));
+  cx<R> mass = scal(mm, scal(rc<R>(4.0f), c0) + E(0, i, j + 1) + E(0, i, j - 1));
   cx<R> cur = scal(kap(i, j), curl<R>(E, i, j)) - scal(kap(i, j - 1), curl<R>(E, i, j - 1));
   return scal(axy, cur) + mass;
 }
 template <typename R, typename A>
 __device__ __forceinline__ cx<R> kx_y(const A& E, const Kap<R>& kap, R axy, R mm, int i, int j) {
   cx<R> c0 = E(1, i, j);
-  cx<R> mass = scal(mm, scal(rfrom<R>(4.0), c0) + E(1, i + 1, j) + E(1, i - 1, j));
+  cx<R> mass = scal(mm, scal(rc<R>(4.0f), c0) + E(1, i + 1, j) + E(1, i - 1, j));
   cx<R> cur = scal(kap(i - 1, j), curl<R>(E, i - 1, j)) - scal(kap(i, j), curl<R>(E, i, j));
   return scal(axy, cur) + mass;
 }
 // mass only (no kappa)
 template <typename R, typename A>
 __device__ __forceinline__ cx<R> mx_x(const A& E, R mm, int i, int j) {
-  return scal(mm, scal(rfrom<R>(4.0), E(0, i, j)) + E(0, i, j + 1) + E(0, i, j - 1));
+  return scal(mm, scal(rc<R>(4.0f), E(0, i, j)) + E(0, i, j + 1) + E(0, i, j - 1));
 }
 template <typename R, typename A>
 __device__ __forceinline__ cx<R> mx_y(const A& E, R mm, int i, int j) {
-  return scal(mm, scal(rfrom<R>(4.0), E(1, i, j)) + E(1, i + 1, j) + E(1, i - 1, j));
+  return scal(mm, scal(rc<R>(4.0f), E(1, i, j)) + E(1, i + 1, j) + E(1, i - 1, j));
 }
 
 
 // ------------------------------------------------------------------
 // edge operator
 // ------------------------------------------------------------------
+// y = cy * (yin ? yin : y) + axy*A x + mm*M x; axy = alpha n^2, mm = beta/6
+// (per (k, v) from beta_kv when given: that form converts in double and
+// serves the shifted operator of the mirror API only)
 template <typename SX, typename SY, typename R>
-__global__ void k_edge_apply(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
-                             double alpha, double beta, const double* __restrict__ beta_kv,
-                             double cy, const SX* __restrict__ x, SY* __restrict__ y) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) n * n * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % n), j = (int) (site / n);
+__global__ void k_edge_apply(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap, Sc axy_s,
+                             Sc mm_s, const double* __restrict__ beta_kv, Sc cy_s, int has_cy,
+                             const SX* __restrict__ x, const SY* yin, SY* y) {
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= n * n) return;
+  int i = site % n, j = site / n;
   Lay L{n, m, K};
-  EAcc<SX, R> E{x + L.edge(k, 0, 0, 0, v), n, m, load_seam<R>(ph, k, n)};
-  R axy = rfrom<R>(alpha * (double) n * (double) n);
-  double b = beta_kv ? beta_kv[(size_t) k * m + v] : beta;
-  R mm = rfrom<R>(b / 6.0);
+  EAcc<SX, R> E{x + L.edge(k, 0, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
+  R axy = sget<R>(axy_s);
+  R mm = beta_kv ? Real<R>::from(beta_kv[(size_t) k * m + v] / 6.0) : sget<R>(mm_s);
   cx<R> ox = kx_x<R>(E, kap, axy, mm, i, j);
   cx<R> oy = kx_y<R>(E, kap, axy, mm, i, j);
-  SY* px = y + L.edge(k, 0, j, i, v);
-  SY* py = y + L.edge(k, 1, j, i, v);
-  if (cy != 0.0) {
-    R c = rfrom<R>(cy);
-    ox += scal(c, Store<SY, R>::ld(px));
-    oy += scal(c, Store<SY, R>::ld(py));
+  size_t ox_at = L.edge(k, 0, j, i, v), oy_at = L.edge(k, 1, j, i, v);
+  if (has_cy) {
+    const SY* src = yin ? yin : y;
+    R c = sget<R>(cy_s);
+    ox += scal(c, Store<SY, R>::ld(src + ox_at));
+    oy += scal(c, Store<SY, R>::ld(src + oy_at));
   }
-  Store<SY, R>::st(px, ox);
-  Store<SY, R>::st(py, oy);
+  Store<SY, R>::st(y + ox_at, ox);
+  Store<SY, R>::st(y + oy_at, oy);
 }
 
 // ------------------------------------------------------------------
@@ -169,10 +166,72 @@ __device__ __forceinline__ void deposit_e(S* base, int n, int m, const Seam<R>& 
   Store<S, R>::st(q, Store<S, R>::ld(q) + val);
 }
 
+// One (k, vector) edge vector with seam phases on load and store: a value
+// addressed one period outside is the stored value times the phase, and is
+// written back multiplied by the conjugate phase.
+template <typename S, typename R>
+struct EIO {
+  S* base;
+  int n, m;
+  Seam<R> seam;
+  __device__ __forceinline__ cx<R> ld(int p, int i, int j) const {
+    cx<R> ph;
+    bool w = seam.wrap(i, j, ph);
+    cx<R> v = Store<S, R>::ld(base + ((size_t) (p * n + j) * n + i) * m);
+    return w ? ph * v : v;
+  }
+  __device__ __forceinline__ void st(int p, int i, int j, cx<R> v) const {
+    cx<R> ph;
+    if (seam.wrap(i, j, ph)) v = conjc(ph) * v;
+    Store<S, R>::st(base + ((size_t) (p * n + j) * n + i) * m, v);
+  }
+};
+
+// Sliding window over a row: the thread holds the patch data of vertex
+// (i,j) -- the reference's mxx[2][3], mxy[3][2], meps[2][2], mbx[2], mby[2]
+// (edge2d.c:2185-2236) -- and moves it by one column per patch, loading the
+// next column only.  Values are written back once no later patch of this row
+// changes them (the ones crossing the periodic seam are written at once, so
+// that the row's last patches read them back updated, as the reference does).
+// The factors of the transformed patch matrix depend on the four cell
+// kappas of the vertex and the scalars only, not on the k-point or vector:
+// for FP32 sweeps they are tabulated once per level (mxk_afw_factors) as
+// (l20, l21, 1/D0, 1/D1) and (1/D2) per vertex, bitwise equal to computing
+// them in the sweep.
+struct AfwF {
+  float l20, l21, i0, i1, i2;
+};
+template <typename R>
+__device__ __forceinline__ void afw_factors(R kLL, R kUL, R kLR, R kUR, R axy, R s8, R& l20, R& l21, R& i0,
+                                            R& i1, R& i2) {
+  R aLL = axy * kLL, aLR = axy * kLR, aUL = axy * kUL, aUR = axy * kUR;
+  R D0 = aUL + aLR + s8;
+  l20 = (aUL - aLR) / D0;
+  R D1 = aLL + aUR;
+  l21 = (aLL - aUR) / D1;
+  R D2 = aLL + aUL + aLR + aUR + s8 - l21 * l21 * D1;
+  const R one = rc<R>(1.0f);
+  i0 = one / D0;
+  i1 = one / D1;
+  i2 = one / D2;
+}
+
+__global__ void k_afw_factors(int n, const float* __restrict__ kap, float axy, float s8, float4* __restrict__ out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  int i = t % n, j = t / n;
+  float kLL = kap[wrapi(i - 1, n) + wrapi(j - 1, n) * n], kUL = kap[wrapi(i - 1, n) + j * n];
+  float kLR = kap[i + wrapi(j - 1, n) * n], kUR = kap[i + j * n];
+  float l20, l21, i0, i1, i2;
+  afw_factors<float>(kLL, kUL, kLR, kUR, axy, s8, l20, l21, i0, i1, i2);
+  out[2 * t] = make_float4(l20, l21, i0, i1);
+  out[2 * t + 1] = make_float4(i2, 0.0f, 0.0f, 0.0f);
+}
+
 template <typename S, typename R>
 __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
-                               double alpha, double beta, int j0, int jstep, int nrows, int backward,
-                               const S* __restrict__ b, S* x) {
+                               const float4* __restrict__ ftab, Sc axy_s, Sc mm_s, Sc s8_s, Sc is8_s, int j0,
+                               int jstep, int nrows, int backward, const S* __restrict__ b, S* x) {
   size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
   size_t per_k = (size_t) nrows * m;
   if (t >= per_k * K) return;
@@ -181,46 +240,111 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
   int v = r % m;
   int j = j0 + (r / m) * jstep;
   Lay L{n, m, K};
-  Seam<R> seam = load_seam<R>(ph, k, n);
-  S* xb = x + L.edge(k, 0, 0, 0, v);
-  EAcc<S, R> X{xb, n, m, seam};
-  EAcc<S, R> B{b + L.edge(k, 0, 0, 0, v), n, m, seam};
-  R axy = rfrom<R>(alpha * (double) n * (double) n);
-  R mm = rfrom<R>(beta / 6.0);
-  R s8 = rfrom<R>(8.0 * beta / 6.0);   // 4 (mx + my), mx = my
-  R quarter = rfrom<R>(0.25);
+  Seam<R> seam = seam_load<R>(ph, K, k, n);
+  EIO<S, R> X{x + L.edge(k, 0, 0, 0, v), n, m, seam};
+  EIO<S, R> B{const_cast<S*>(b) + L.edge(k, 0, 0, 0, v), n, m, seam};
+  const R axy = sget<R>(axy_s);
+  const R mm = sget<R>(mm_s);
+  const R s8 = sget<R>(s8_s);     // 4 (mx + my), mx = my
+  const R is8 = sget<R>(is8_s);
+  const R four = rc<R>(4.0f), quarter = rc<R>(0.25f);
+  const bool tab = ftab != nullptr;
+  int i = backward ? n - 1 : 0;
+  // x columns i-1 (a) and i (b), rows j-1, j, j+1; y columns i-1 (a), i (b), i+1 (c), rows j-1, j
+  cx<R> xa0 = X.ld(0, i - 1, j - 1), xa1 = X.ld(0, i - 1, j), xa2 = X.ld(0, i - 1, j + 1);
+  cx<R> xb0 = X.ld(0, i, j - 1), xb1 = X.ld(0, i, j), xb2 = X.ld(0, i, j + 1);
+  cx<R> ya0 = X.ld(1, i - 1, j - 1), ya1 = X.ld(1, i - 1, j);
+  cx<R> yb0 = X.ld(1, i, j - 1), yb1 = X.ld(1, i, j);
+  cx<R> yc0 = X.ld(1, i + 1, j - 1), yc1 = X.ld(1, i + 1, j);
+  R kLL = kap(i - 1, j - 1), kUL = kap(i - 1, j), kLR = kap(i, j - 1), kUR = kap(i, j);
+  cx<R> bx0 = B.ld(0, i - 1, j), bx1 = B.ld(0, i, j), by0 = B.ld(1, i, j - 1), by1 = B.ld(1, i, j);
+  float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fb = fa;
+  if (tab) { fa = ftab[2 * ((size_t) j * n + i)]; fb = ftab[2 * ((size_t) j * n + i) + 1]; }
   for (int step = 0; step < n; step++) {
-    int i = backward ? n - 1 - step : step;
-    R kLL = axy * kap(i - 1, j - 1), kLR = axy * kap(i, j - 1);
-    R kUL = axy * kap(i - 1, j), kUR = axy * kap(i, j);
-    // transformed local matrix (mx = my: T10 = T32 = 0)
-    R T00 = kUL + kLR + s8, T20 = kUL - kLR;
-    R T11 = kLL + kUR, T21 = kLL - kUR;
-    R T22 = kLL + kUL + kLR + kUR + s8, T33 = s8;
-    // L D L^T with the reference's elimination (no l20 fill in entry (2,2))
-    R D0 = T00, l20 = T20 / D0;
-    R D1 = T11, l21 = T21 / D1;
-    R D2 = T22 - l21 * l21 * D1;
-    R D3 = T33;
-    cx<R> r0 = B(0, i - 1, j) - kx_x<R>(X, kap, axy, mm, i - 1, j);
-    cx<R> r1 = B(0, i, j) - kx_x<R>(X, kap, axy, mm, i, j);
-    cx<R> r2 = B(1, i, j - 1) - kx_y<R>(X, kap, axy, mm, i, j - 1);
-    cx<R> r3 = B(1, i, j) - kx_y<R>(X, kap, axy, mm, i, j);
+    const bool last = step == n - 1;
+    // prefetch the column the next patch adds (never written by this patch)
+    cx<R> nx0, nx1, nx2, ny0, ny1, nbx, nby0, nby1;
+    R nk0, nk1;
+    float4 nfa, nfb;
+    if (!last) {
+      int ix = backward ? i - 2 : i + 1;    // new x column
+      int iy = backward ? i - 2 : i + 2;    // new y column
+      int ib = backward ? i - 1 : i + 1;    // new patch column
+      nx0 = X.ld(0, ix, j - 1); nx1 = X.ld(0, ix, j); nx2 = X.ld(0, ix, j + 1);
+      ny0 = X.ld(1, iy, j - 1); ny1 = X.ld(1, iy, j);
+      nk0 = kap(ix, j - 1); nk1 = kap(ix, j);
+      if (tab) {
+        nfa = ftab[2 * ((size_t) j * n + ib)];
+        nfb = ftab[2 * ((size_t) j * n + ib) + 1];
+      }
+      nbx = B.ld(0, backward ? i - 2 : i + 1, j);
+      nby0 = B.ld(1, ib, j - 1); nby1 = B.ld(1, ib, j);
+    }
+    // residual b - (alpha A + beta M) x at the patch unknowns u0..u3 =
+    // x(i-1,j), x(i,j), y(i,j-1), y(i,j) from the four cell curls
+    cx<R> cLL = xa0 - xa1 - ya0 + yb0;
+    cx<R> cUL = xa1 - xa2 - ya1 + yb1;
+    cx<R> cLR = xb0 - xb1 - yb0 + yc0;
+    cx<R> cUR = xb1 - xb2 - yb1 + yc1;
+    cx<R> r0 = bx0 - (scal(axy, scal(kUL, cUL) - scal(kLL, cLL)) + scal(mm, scal(four, xa1) + xa2 + xa0));
+    cx<R> r1 = bx1 - (scal(axy, scal(kUR, cUR) - scal(kLR, cLR)) + scal(mm, scal(four, xb1) + xb2 + xb0));
+    cx<R> r2 = by0 - (scal(axy, scal(kLL, cLL) - scal(kLR, cLR)) + scal(mm, scal(four, yb0) + yc0 + ya0));
+    cx<R> r3 = by1 - (scal(axy, scal(kUL, cUL) - scal(kUR, cUR)) + scal(mm, scal(four, yb1) + yc1 + ya1));
+    // transformed local matrix (mx = my: T10 = T32 = 0) and the reference's
+    // elimination without the l20 fill of entry (2,2)
+    R l20, l21, i0, i1, i2;
+    if (tab) {
+      l20 = Real<R>::from_float(fa.x); l21 = Real<R>::from_float(fa.y);
+      i0 = Real<R>::from_float(fa.z); i1 = Real<R>::from_float(fa.w); i2 = Real<R>::from_float(fb.x);
+    } else {
+      afw_factors<R>(kLL, kUL, kLR, kUR, axy, s8, l20, l21, i0, i1, i2);
+    }
     cx<R> c0 = r0 + r1 + r2 + r3;
     cx<R> c1 = r0 + r1 - r2 - r3;
     cx<R> c2 = r0 - r1 - r2 + r3;
     cx<R> c3 = r0 - r1 + r2 - r3;
     c2 -= scal(l20, c0) + scal(l21, c1);
-    c0 = scal(rfrom<R>(1.0) / D0, c0);
-    c1 = scal(rfrom<R>(1.0) / D1, c1);
-    c2 = scal(rfrom<R>(1.0) / D2, c2);
-    c3 = scal(rfrom<R>(1.0) / D3, c3);
+    c0 = scal(i0, c0);
+    c1 = scal(i1, c1);
+    c2 = scal(i2, c2);
+    c3 = scal(is8, c3);
     c1 -= scal(l21, c2);
     c0 -= scal(l20, c2);
-    deposit_e<S, R>(xb, n, m, seam, 0, i - 1, j, scal(quarter, c0 + c1 + c2 + c3));
-    deposit_e<S, R>(xb, n, m, seam, 0, i, j, scal(quarter, c0 + c1 - c2 - c3));
-    deposit_e<S, R>(xb, n, m, seam, 1, i, j - 1, scal(quarter, c0 - c1 - c2 + c3));
-    deposit_e<S, R>(xb, n, m, seam, 1, i, j, scal(quarter, c0 - c1 + c2 - c3));
+    xa1 += scal(quarter, c0 + c1 + c2 + c3);
+    xb1 += scal(quarter, c0 + c1 - c2 - c3);
+    yb0 += scal(quarter, c0 - c1 - c2 + c3);
+    yb1 += scal(quarter, c0 - c1 + c2 - c3);
+    X.st(1, i, j - 1, yb0);
+    X.st(1, i, j, yb1);
+    if (!backward) {
+      X.st(0, i - 1, j, xa1);
+      if (last) {
+        X.st(0, i, j, xb1);
+        break;
+      }
+      xa0 = xb0; xa1 = xb1; xa2 = xb2;
+      xb0 = nx0; xb1 = nx1; xb2 = nx2;
+      ya0 = yb0; ya1 = yb1; yb0 = yc0; yb1 = yc1;
+      yc0 = ny0; yc1 = ny1;
+      kLL = kLR; kUL = kUR; kLR = nk0; kUR = nk1;
+      if (tab) { fa = nfa; fb = nfb; }
+      bx0 = bx1; bx1 = nbx; by0 = nby0; by1 = nby1;
+      i++;
+    } else {
+      X.st(0, i, j, xb1);
+      if (last) {
+        X.st(0, i - 1, j, xa1);
+        break;
+      }
+      xb0 = xa0; xb1 = xa1; xb2 = xa2;
+      xa0 = nx0; xa1 = nx1; xa2 = nx2;
+      yc0 = yb0; yc1 = yb1; yb0 = ya0; yb1 = ya1;
+      ya0 = ny0; ya1 = ny1;
+      kLR = kLL; kUR = kUL; kLL = nk0; kUL = nk1;
+      if (tab) { fa = nfa; fb = nfb; }
+      bx1 = bx0; bx0 = nbx; by0 = nby0; by1 = nby1;
+      i--;
+    }
   }
 }
 
@@ -228,21 +352,18 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
 // edge transfers (gather form of prolongation_edge2d / restriction_edge2d)
 // ------------------------------------------------------------------
 template <typename S, typename R>
-__global__ void k_edge_prolong(int nc, int m, int K, const double* __restrict__ ph, double alpha,
+__global__ void k_edge_prolong(int nc, int m, int K, const double* __restrict__ ph, Sc alpha,
                                const S* __restrict__ c, S* __restrict__ f) {
   int nf = 2 * nc;
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) nf * nf * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % nf), j = (int) (site / nf);
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nf * nf) return;
+  int i = site % nf, j = site / nf;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  EAcc<S, R> C{c + Lc.edge(k, 0, 0, 0, v), nc, m, load_seam<R>(ph, k, nc)};
+  EAcc<S, R> C{c + Lc.edge(k, 0, 0, 0, v), nc, m, seam_load<R>(ph, K, k, nc)};
   int ci = i >> 1, cj = j >> 1;
-  R half = rfrom<R>(0.5), quarter = rfrom<R>(0.25), a = rfrom<R>(alpha);
+  R half = rc<R>(0.5f), quarter = rc<R>(0.25f), a = sget<R>(alpha);
   cx<R> vx = (j & 1) ? scal(quarter, C(0, ci, cj) + C(0, ci, cj + 1)) : scal(half, C(0, ci, cj));
   cx<R> vy = (i & 1) ? scal(quarter, C(1, ci, cj) + C(1, ci + 1, cj)) : scal(half, C(1, ci, cj));
   S* px = f + Lf.edge(k, 0, j, i, v);
@@ -252,20 +373,17 @@ __global__ void k_edge_prolong(int nc, int m, int K, const double* __restrict__ 
 }
 
 template <typename S, typename R>
-__global__ void k_edge_restrict(int nc, int m, int K, const double* __restrict__ ph, double alpha,
+__global__ void k_edge_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc alpha,
                                 const S* __restrict__ f, S* __restrict__ c) {
   int nf = 2 * nc;
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) nc * nc * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % nc), j = (int) (site / nc);
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nc * nc) return;
+  int i = site % nc, j = site / nc;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  EAcc<S, R> F{f + Lf.edge(k, 0, 0, 0, v), nf, m, load_seam<R>(ph, k, nf)};
-  R half = rfrom<R>(0.5), quarter = rfrom<R>(0.25), a = rfrom<R>(alpha);
+  EAcc<S, R> F{f + Lf.edge(k, 0, 0, 0, v), nf, m, seam_load<R>(ph, K, k, nf)};
+  R half = rc<R>(0.5f), quarter = rc<R>(0.25f), a = sget<R>(alpha);
   int fi = 2 * i, fj = 2 * j;
   cx<R> sx = scal(half, F(0, fi, fj) + F(0, fi + 1, fj))
              + scal(quarter, F(0, fi, fj - 1) + F(0, fi + 1, fj - 1) + F(0, fi, fj + 1) + F(0, fi + 1, fj + 1));
@@ -287,109 +405,162 @@ __device__ __forceinline__ cx<R> lap_off(const A& V, int i, int j) {
 }
 
 template <typename S, typename R>
-__global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph, double alpha,
-                             double cy, const S* __restrict__ x, S* __restrict__ y) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) n * n * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % n), j = (int) (site / n);
+__global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph, Sc diag, Sc off, Sc cy,
+                             int has_cy, const S* __restrict__ x, const S* yin, S* y) {
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= n * n) return;
+  int i = site % n, j = site / n;
   Lay L{n, m, K};
-  NAcc<S, R> V{x + L.node(k, 0, 0, v), n, m, load_seam<R>(ph, k, n)};
-  cx<R> o = scal(rfrom<R>(alpha * 8.0 / 3.0), V(i, j)) + scal(rfrom<R>(-alpha / 3.0), lap_off<R>(V, i, j));
-  S* py = y + L.node(k, j, i, v);
-  if (cy != 0.0) o += scal(rfrom<R>(cy), Store<S, R>::ld(py));
-  Store<S, R>::st(py, o);
+  NAcc<S, R> V{x + L.node(k, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
+  cx<R> o = scal(sget<R>(diag), V(i, j)) + scal(sget<R>(off), lap_off<R>(V, i, j));
+  size_t at = L.node(k, j, i, v);
+  if (has_cy) o += scal(sget<R>(cy), Store<S, R>::ld((yin ? yin : y) + at));
+  Store<S, R>::st(y + at, o);
 }
 
 template <typename S, typename R>
-__global__ void k_node_gs_rows(int n, int m, int K, const double* __restrict__ ph, double alpha,
-                               int j0, int jstep, int nrows, int backward, const S* __restrict__ b,
-                               S* x) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) nrows * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  int r = (int) (t - (size_t) k * per_k);
-  int v = r % m;
-  int j = j0 + (r / m) * jstep;
+struct NIO {
+  S* base;
+  int n, m;
+  Seam<R> seam;
+  __device__ __forceinline__ cx<R> ld(int i, int j) const {
+    cx<R> ph;
+    bool w = seam.wrap(i, j, ph);
+    cx<R> v = Store<S, R>::ld(base + ((size_t) j * n + i) * m);
+    return w ? ph * v : v;
+  }
+  __device__ __forceinline__ void st(int i, int j, cx<R> v) const {
+    cx<R> ph;
+    if (seam.wrap(i, j, ph)) v = conjc(ph) * v;
+    Store<S, R>::st(base + ((size_t) j * n + i) * m, v);
+  }
+};
+
+// Point Gauss-Seidel of one row, solved in parallel.  Along a row the sweep
+// is x_i = x_{i-s}/8 + beta_i (s = +1 forward, -1 backward): the coefficient
+// of the already updated neighbour is (1/3)*(3/8) = 1/8 for any alpha, and
+// beta_i = (3/(8 alpha)) (b_i + (alpha/3) * (old right neighbour + the six
+// neighbours in rows j-1, j+1)).  The chain starts at i0 with the old value
+// across the seam (folded into beta'_{i0} = beta_{i0} + x_{i0-s}/8) and ends
+// with the new x_{i0} across the seam.  Hence
+//   x_{i_t} = sum_{d=0}^{min(t,D)} 8^-d beta'_{i_{t-d}},
+// truncated where 8^-(D+1) is below the arithmetic's precision.
+// One CTA per (row, k-point) walks its row in segments of NSEG chain
+// positions: pass 1 puts beta' of the segment into a ring in shared memory
+// (reading old values only: the row's own x is rewritten one segment at a
+// time, behind every position pass 1 still reads), pass 2 writes the
+// truncated prefix sums into x.  The new x_{i0} that the last position
+// needs is formed from old values before anything is written.
+constexpr int NSEG = 64, NRING = 88;
+
+template <typename S, typename R, int D>
+__global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s,
+                              int j0, int jstep, int backward, const S* __restrict__ b, S* x) {
+  static_assert(NRING >= NSEG + D, "ring too short for the prefix depth");
+  extern __shared__ float smn[];
+  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);   // NRING * m
+  cx<R>* x0s = ring + NRING * m;                  // m
+  int k = blockIdx.y, v = threadIdx.x, P = blockDim.y, ty = threadIdx.y;
+  int j = j0 + blockIdx.x * jstep;
   Lay L{n, m, K};
-  S* xb = x + L.node(k, 0, 0, v);
-  NAcc<S, R> V{xb, n, m, load_seam<R>(ph, k, n)};
+  Seam<R> seam = seam_load<R>(ph, K, k, n);
+  NAcc<S, R> X{x + L.node(k, 0, 0, v), n, m, seam};
+  S* xr = x + L.node(k, j, 0, v);
   const S* bb = b + L.node(k, 0, 0, v);
-  R inv_ac = rfrom<R>(3.0 / (8.0 * alpha));
-  R ao = rfrom<R>(-alpha / 3.0);
-  for (int step = 0; step < n; step++) {
-    int i = backward ? n - 1 - step : step;
-    cx<R> rhs = Store<S, R>::ld(bb + ((size_t) j * n + i) * m) - scal(ao, lap_off<R>(V, i, j));
-    Store<S, R>::st(xb + ((size_t) j * n + i) * m, scal(inv_ac, rhs));
+  const int sd = backward ? -1 : 1, i0 = backward ? n - 1 : 0;
+  const R inv_ac = sget<R>(inv_ac_s), third = sget<R>(third_s), eighth = rc<R>(0.125f);
+  auto beta_at = [&](int ii, cx<R> next) {
+    cx<R> nb = next + X(ii - 1, j - 1) + X(ii, j - 1) + X(ii + 1, j - 1) + X(ii - 1, j + 1) + X(ii, j + 1)
+               + X(ii + 1, j + 1);
+    return scal(inv_ac, Store<S, R>::ld(bb + ((size_t) j * n + ii) * m) + scal(third, nb));
+  };
+  if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
+  __syncthreads();
+  for (int t0 = 0; t0 < n; t0 += NSEG) {
+    int t1 = t0 + NSEG < n ? t0 + NSEG : n;
+    for (int t = t0 + ty; t < t1; t += P) {
+      int i = i0 + sd * t;
+      cx<R> out;
+      if (t == 0) {
+        out = x0s[v];
+      } else if (t == n - 1) {
+        cx<R> phz;
+        int ii = i + sd, jj = j;
+        bool w = seam.wrap(ii, jj, phz);
+        out = beta_at(i, w ? phz * x0s[v] : x0s[v]);
+      } else {
+        out = beta_at(i, X(i + sd, j));
+      }
+      ring[(t % NRING) * m + v] = out;
+    }
+    __syncthreads();
+    for (int t = t0 + ty; t < t1; t += P) {
+      cx<R> acc = czero<R>();
+      int dmax = t < D ? t : D;
+      for (int d = dmax; d >= 0; d--)   // Horner from the farthest term
+        acc = scal(eighth, acc) + ring[((t - d) % NRING) * m + v];
+      Store<S, R>::st(xr + (size_t) (i0 + sd * t) * m, acc);
+    }
+    __syncthreads();
   }
 }
 
 template <typename S, typename R>
-__global__ void k_node_prolong(int nc, int m, int K, const double* __restrict__ ph, double alpha,
+__global__ void k_node_prolong(int nc, int m, int K, const double* __restrict__ ph, Sc alpha,
                                const S* __restrict__ c, S* __restrict__ f) {
   int nf = 2 * nc;
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) nf * nf * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % nf), j = (int) (site / nf);
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nf * nf) return;
+  int i = site % nf, j = site / nf;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  NAcc<S, R> C{c + Lc.node(k, 0, 0, v), nc, m, load_seam<R>(ph, k, nc)};
+  NAcc<S, R> C{c + Lc.node(k, 0, 0, v), nc, m, seam_load<R>(ph, K, k, nc)};
   int ci = i >> 1, cj = j >> 1, oi = i & 1, oj = j & 1;
   cx<R> val = C(ci, cj);
   if (oi) val += C(ci + 1, cj);
   if (oj) val += C(ci, cj + 1);
   if (oi && oj) val += C(ci + 1, cj + 1);
-  double w = alpha * (oi ? 0.5 : 1.0) * (oj ? 0.5 : 1.0);
+  // weight alpha * (1/2 per odd coordinate): exact powers of two
+  if (oi) val = scal(rc<R>(0.5f), val);
+  if (oj) val = scal(rc<R>(0.5f), val);
   S* p = f + Lf.node(k, j, i, v);
-  Store<S, R>::st(p, Store<S, R>::ld(p) + scal(rfrom<R>(w), val));
+  Store<S, R>::st(p, Store<S, R>::ld(p) + scal(sget<R>(alpha), val));
 }
 
 template <typename S, typename R>
-__global__ void k_node_restrict(int nc, int m, int K, const double* __restrict__ ph, double alpha,
+__global__ void k_node_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc alpha,
                                 const S* __restrict__ f, S* __restrict__ c) {
   int nf = 2 * nc;
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) nc * nc * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % nc), j = (int) (site / nc);
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nc * nc) return;
+  int i = site % nc, j = site / nc;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  NAcc<S, R> F{f + Lf.node(k, 0, 0, v), nf, m, load_seam<R>(ph, k, nf)};
+  NAcc<S, R> F{f + Lf.node(k, 0, 0, v), nf, m, seam_load<R>(ph, K, k, nf)};
   int fi = 2 * i, fj = 2 * j;
   cx<R> s = F(fi, fj)
-            + scal(rfrom<R>(0.5), F(fi - 1, fj) + F(fi + 1, fj) + F(fi, fj - 1) + F(fi, fj + 1))
-            + scal(rfrom<R>(0.25), F(fi - 1, fj - 1) + F(fi + 1, fj - 1) + F(fi - 1, fj + 1) + F(fi + 1, fj + 1));
+            + scal(rc<R>(0.5f), F(fi - 1, fj) + F(fi + 1, fj) + F(fi, fj - 1) + F(fi, fj + 1))
+            + scal(rc<R>(0.25f), F(fi - 1, fj - 1) + F(fi + 1, fj - 1) + F(fi - 1, fj + 1) + F(fi + 1, fj + 1));
   S* p = c + Lc.node(k, j, i, v);
-  Store<S, R>::st(p, Store<S, R>::ld(p) + scal(rfrom<R>(alpha), s));
+  Store<S, R>::st(p, Store<S, R>::ld(p) + scal(sget<R>(alpha), s));
 }
 
 template <typename SV, typename SE, typename R>
-__global__ void k_gradient(int n, int m, int K, const double* __restrict__ ph, double alpha,
+__global__ void k_gradient(int n, int m, int K, const double* __restrict__ ph, Sc alpha,
                            const SV* __restrict__ vin, SE* __restrict__ e) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) n * n * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % n), j = (int) (site / n);
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= n * n) return;
+  int i = site % n, j = site / n;
   Lay L{n, m, K};
-  NAcc<SV, R> V{vin + L.node(k, 0, 0, v), n, m, load_seam<R>(ph, k, n)};
+  NAcc<SV, R> V{vin + L.node(k, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
   cx<R> c = V(i, j);
-  R a = rfrom<R>(alpha);
+  R a = sget<R>(alpha);
   SE* px = e + L.edge(k, 0, j, i, v);
   SE* py = e + L.edge(k, 1, j, i, v);
   Store<SE, R>::st(px, Store<SE, R>::ld(px) + scal(a, V(i + 1, j) - c));
@@ -397,22 +568,19 @@ __global__ void k_gradient(int n, int m, int K, const double* __restrict__ ph, d
 }
 
 template <typename SE, typename SV, typename R>
-__global__ void k_adjgradient(int n, int m, int K, const double* __restrict__ ph, double alpha,
-                              int mass, double cv, const SE* __restrict__ e, SV* __restrict__ vout) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  size_t per_k = (size_t) n * n * m;
-  if (t >= per_k * K) return;
-  int k = (int) (t / per_k);
-  size_t r = t - (size_t) k * per_k;
-  int v = (int) (r % m);
-  size_t site = r / m;
-  int i = (int) (site % n), j = (int) (site / n);
+__global__ void k_adjgradient(int n, int m, int K, const double* __restrict__ ph, Sc alpha, int mass,
+                              Sc sixth, Sc cv, int has_cv, const SE* __restrict__ e, SV* __restrict__ vout) {
+  // block (m, rows): x = vector, y = site; grid.y = k-point
+  int k = blockIdx.y, v = threadIdx.x;
+  int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= n * n) return;
+  int i = site % n, j = site / n;
   Lay L{n, m, K};
-  EAcc<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, load_seam<R>(ph, k, n)};
+  EAcc<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
   cx<R> s;
   if (mass) {
     // G^H M e: the mass stencil evaluated at the four edges of the node
-    R mm = rfrom<R>(1.0 / 6.0);
+    R mm = sget<R>(sixth);
     s = mx_x<R>(E, mm, i - 1, j);
     // the left x-edge value must carry the seam phase of position i-1
     if (i == 0) {
@@ -430,20 +598,14 @@ __global__ void k_adjgradient(int n, int m, int K, const double* __restrict__ ph
     s = E(0, i - 1, j) - E(0, i, j) + E(1, i, j - 1) - E(1, i, j);
   }
   SV* p = vout + L.node(k, j, i, v);
-  cx<R> o = scal(rfrom<R>(alpha), s);
-  if (cv != 0.0) o += scal(rfrom<R>(cv), Store<SV, R>::ld(p));
+  cx<R> o = scal(sget<R>(alpha), s);
+  if (has_cv) o += scal(sget<R>(cv), Store<SV, R>::ld(p));
   Store<SV, R>::st(p, o);
 }
 
 // ------------------------------------------------------------------
 // block BLAS-1
 // ------------------------------------------------------------------
-template <typename S>
-__global__ void k_zero(S* x, size_t len) {
-  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < len) memset(x + t, 0, sizeof(S));
-}
-
 template <typename SX, typename SY, typename R>
 __global__ void k_convert(const SX* __restrict__ x, SY* __restrict__ y, size_t len) {
   size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -451,46 +613,61 @@ __global__ void k_convert(const SX* __restrict__ x, SY* __restrict__ y, size_t l
 }
 
 template <typename SX, typename SY, typename R>
-__global__ void k_axpy(double are, double aim, const SX* __restrict__ x, SY* __restrict__ y, size_t len) {
+__global__ void k_axpy(Sc are, Sc aim, const SX* __restrict__ x, SY* __restrict__ y, size_t len) {
   size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (t < len) {
-    cx<R> a = cfrom<R>(are, aim);
+    cx<R> a = mkc(sget<R>(are), sget<R>(aim));
     Store<SY, R>::st(y + t, Store<SY, R>::ld(y + t) + a * Store<SX, R>::ld(x + t));
   }
 }
 
-// mean of each plane of each (k, v): one block per (k, plane), m <= 32 lanes of v
+// mean of each plane of each (k, v), in two passes: partial sums of a chunk
+// of sites per block added atomically into acc[(k*2+p)*m+v] (re, im), then
+// the subtraction; only k-points whose flag is set are touched
 template <typename S, typename R>
-__global__ void k_center(int n, int m, int K, const int* __restrict__ gamma, S* x) {
-  int k = blockIdx.x / 2, p = blockIdx.x % 2;
+__global__ void k_center_sum(int n, int m, int K, const int* __restrict__ gamma, const S* __restrict__ x,
+                             double* acc) {
+  int k = blockIdx.y / 2, p = blockIdx.y % 2;
   if (!gamma[k]) return;
   Lay L{n, m, K};
-  __shared__ double sre[256], sim[256];
-  int v = threadIdx.x % m, row = threadIdx.x / m, rows = blockDim.x / m;
+  int v = threadIdx.x, row = threadIdx.y, rows = blockDim.y;
   double are = 0.0, aim = 0.0;
-  if (row < rows) {
-    for (size_t s = row; s < (size_t) n * n; s += rows) {
-      cx<R> val = Store<S, R>::ld(x + L.edge(k, p, 0, 0, v) + s * m);
-      are += Real<R>::to_double(val.re);
-      aim += Real<R>::to_double(val.im);
-    }
+  for (int s = blockIdx.x * rows + row; s < n * n; s += gridDim.x * rows) {
+    cx<double> val = Store<S, double>::ld(x + L.edge(k, p, 0, 0, v) + (size_t) s * m);
+    are += val.re;
+    aim += val.im;
   }
-  sre[threadIdx.x] = are;
-  sim[threadIdx.x] = aim;
+  __shared__ double sre[256], sim[256];
+  int t = threadIdx.y * blockDim.x + threadIdx.x;
+  sre[t] = are;
+  sim[t] = aim;
   __syncthreads();
-  if (threadIdx.x < m) {
+  if (threadIdx.y == 0) {
     double tr = 0.0, ti = 0.0;
-    for (int q = threadIdx.x; q < rows * m; q += m) { tr += sre[q]; ti += sim[q]; }
-    sre[threadIdx.x] = tr / ((double) n * n);
-    sim[threadIdx.x] = ti / ((double) n * n);
+    for (int r = 0; r < rows; r++) { tr += sre[r * blockDim.x + v]; ti += sim[r * blockDim.x + v]; }
+    atomicAdd(acc + 2 * ((size_t) (k * 2 + p) * m + v), tr);
+    atomicAdd(acc + 2 * ((size_t) (k * 2 + p) * m + v) + 1, ti);
   }
+}
+
+template <typename S, typename R>
+__global__ void k_center_sub(int n, int m, int K, const int* __restrict__ gamma, const double* __restrict__ acc,
+                             S* x) {
+  int k = blockIdx.y / 2, p = blockIdx.y % 2;
+  if (!gamma[k]) return;
+  int v = threadIdx.x;
+  int s = blockIdx.x * blockDim.y + threadIdx.y;
+  Lay L{n, m, K};
+  const double* a = acc + 2 * ((size_t) (k * 2 + p) * m + v);
+  // one row of threads forms the block's means (m <= 32), so that the double
+  // division and conversion run once per block rather than once per entry
+  __shared__ cx<R> mean_s[32];
+  if (threadIdx.y == 0) mean_s[v] = cfrom<R>(a[0] / ((double) n * n), a[1] / ((double) n * n));
   __syncthreads();
-  cx<R> mean = cfrom<R>(sre[v], sim[v]);
-  if (row < rows)
-    for (size_t s = row; s < (size_t) n * n; s += rows) {
-      S* q = x + L.edge(k, p, 0, 0, v) + s * m;
-      Store<S, R>::st(q, Store<S, R>::ld(q) - mean);
-    }
+  if (s >= n * n) return;
+  cx<R> mean = mean_s[v];
+  S* q = x + L.edge(k, p, 0, 0, v) + (size_t) s * m;
+  Store<S, R>::st(q, Store<S, R>::ld(q) - mean);
 }
 
 // ------------------------------------------------------------------
@@ -527,7 +704,7 @@ __global__ void k_dense_edge(int n, int K, const double* __restrict__ ph, Kap<do
   int rc = (int) (t % ((size_t) N * N));
   int row = rc % N, col = rc / N;
   int nn = n * n;
-  UnitEdge E{n, col / nn, (col % nn) % n, (col % nn) / n, load_seam<double>(ph, k, n)};
+  UnitEdge E{n, col / nn, (col % nn) % n, (col % nn) / n, seam_load<double>(ph, K, k, n)};
   int rp = row / nn, ri = (row % nn) % n, rj = (row % nn) / n;
   double axy = alpha * n * (double) n, mm = beta / 6.0;
   cx<double> val = rp == 0 ? kx_x<double>(E, kap, axy, mm, ri, rj) : kx_y<double>(E, kap, axy, mm, ri, rj);
@@ -543,7 +720,7 @@ __global__ void k_dense_node(int n, int K, const double* __restrict__ ph, int fi
   int k = (int) (t / ((size_t) N * N));
   int rc = (int) (t % ((size_t) N * N));
   int row = rc % N, col = rc / N;
-  Seam<double> seam = load_seam<double>(ph, k, n);
+  Seam<double> seam = seam_load<double>(ph, K, k, n);
   UnitNode V{n, col % n, col / n, seam};
   int ri = row % n, rj = row / n;
   cx<double> val = scal(8.0 / 3.0, V(ri, rj)) + scal(-1.0 / 3.0, lap_off<double>(V, ri, rj));
@@ -601,85 +778,130 @@ static int L_edge_gs_rows(int n, int m, int K, const double* ph, mxk_kappa kap, 
                           double beta, int j0, int jstep, int nrows, int backward, const void* b,
                           void* x, cudaStream_t st) {
   size_t work = (size_t) nrows * m * K;
-  k_edge_gs_rows<S, R><<<nblocks(work, 64), 64, 0, st>>>(n, m, K, ph, make_kap<R>(kap, n), alpha, beta,
-                                                         j0, jstep, nrows, backward, (const S*) b, (S*) x);
+  // the tabulated factors serve FP32 sweeps with the scalars they were made for
+  const float4* ftab = (sizeof(R) == 4 && kap.afw && kap.afw_alpha == alpha && kap.afw_beta == beta)
+                           ? (const float4*) kap.afw : nullptr;
+  k_edge_gs_rows<S, R><<<nblocks(work, 64), 64, 0, st>>>(
+      n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
+      make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), j0, jstep, nrows, backward, (const S*) b, (S*) x);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_edge_prolong(int nc, int m, int K, const double* ph, double alpha, const void* c, void* f,
                           cudaStream_t st) {
-  k_edge_prolong<S, R><<<nblocks((size_t) 4 * nc * nc * m * K), TPB, 0, st>>>(nc, m, K, ph, alpha, (const S*) c, (S*) f);
+  k_edge_prolong<S, R><<<grd2((size_t) 4 * nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
+                                                                             (const S*) c, (S*) f);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_edge_restrict(int nc, int m, int K, const double* ph, double alpha, const void* f, void* c,
                            cudaStream_t st) {
-  k_edge_restrict<S, R><<<nblocks((size_t) nc * nc * m * K), TPB, 0, st>>>(nc, m, K, ph, alpha, (const S*) f, (S*) c);
+  k_edge_restrict<S, R><<<grd2((size_t) nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
+                                                                          (const S*) f, (S*) c);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_node_apply(int n, int m, int K, const double* ph, double alpha, double cy, const void* x,
-                        void* y, cudaStream_t st) {
-  k_node_apply<S, R><<<nblocks((size_t) n * n * m * K), TPB, 0, st>>>(n, m, K, ph, alpha, cy, (const S*) x, (S*) y);
+                        const void* yin, void* y, cudaStream_t st) {
+  k_node_apply<S, R><<<grd2((size_t) n * n, m, K), blk2(m), 0, st>>>(
+      n, m, K, ph, make_sc(alpha * 8.0 / 3.0), make_sc(-alpha / 3.0), make_sc(cy), cy != 0.0, (const S*) x,
+      (const S*) yin, (S*) y);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, int j0, int jstep,
                           int nrows, int backward, const void* b, void* x, cudaStream_t st) {
-  k_node_gs_rows<S, R><<<nblocks((size_t) nrows * m * K, 64), 64, 0, st>>>(n, m, K, ph, alpha, j0, jstep, nrows,
-                                                                          backward, (const S*) b, (S*) x);
+  dim3 g(nrows, K), b2 = blk2(m);
+  size_t smem = (size_t) (NRING + 1) * m * sizeof(cx<R>);
+  Sc inv_ac = make_sc(3.0 / (8.0 * alpha)), third = make_sc(alpha / 3.0);
+  // 8^-(D+1) below the unit roundoff: D = 8 for FP32, 18 for FP64 and float-float
+  if (sizeof(R) == 4) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_node_gs_row<S, R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_node_gs_row<S, R, 8><<<g, b2, smem, st>>>(n, m, K, ph, inv_ac, third, j0, jstep, backward, (const S*) b,
+                                                (S*) x);
+  } else {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_node_gs_row<S, R, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_node_gs_row<S, R, 18><<<g, b2, smem, st>>>(n, m, K, ph, inv_ac, third, j0, jstep, backward, (const S*) b,
+                                                 (S*) x);
+  }
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_node_prolong(int nc, int m, int K, const double* ph, double alpha, const void* c, void* f,
                           cudaStream_t st) {
-  k_node_prolong<S, R><<<nblocks((size_t) 4 * nc * nc * m * K), TPB, 0, st>>>(nc, m, K, ph, alpha, (const S*) c, (S*) f);
+  k_node_prolong<S, R><<<grd2((size_t) 4 * nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
+                                                                             (const S*) c, (S*) f);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_node_restrict(int nc, int m, int K, const double* ph, double alpha, const void* f, void* c,
                            cudaStream_t st) {
-  k_node_restrict<S, R><<<nblocks((size_t) nc * nc * m * K), TPB, 0, st>>>(nc, m, K, ph, alpha, (const S*) f, (S*) c);
+  k_node_restrict<S, R><<<grd2((size_t) nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
+                                                                          (const S*) f, (S*) c);
   MX_CHECK_LAUNCH();
   return 0;
 }
 template <typename S, typename R>
 static int L_zero(void* x, size_t len, cudaStream_t st) {
-  k_zero<S><<<nblocks(len), TPB, 0, st>>>((S*) x, len);
+  return (int) cudaMemsetAsync(x, 0, len * sizeof(S), st);
+}
+template <typename S, typename R>
+static int L_center(int n, int m, int K, const int* gamma, void* x, double* acc, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(double) * 4 * (size_t) K * m, st);
+  if (e) return (int) e;
+  unsigned chunks = (unsigned) ((n * n + 4095) / 4096);
+  k_center_sum<S, R><<<dim3(chunks, 2 * K), blk2(m), 0, st>>>(n, m, K, gamma, (const S*) x, acc);
+  MX_CHECK_LAUNCH();
+  unsigned rows = 256 / m;
+  k_center_sub<S, R><<<dim3((n * n + rows - 1) / rows, 2 * K), blk2(m), 0, st>>>(n, m, K, gamma, acc, (S*) x);
   MX_CHECK_LAUNCH();
   return 0;
 }
-template <typename S, typename R>
-static int L_center(int n, int m, int K, const int* gamma, void* x, cudaStream_t st) {
-  int threads = (256 / m) * m;
-  k_center<S, R><<<2 * K, threads, 0, st>>>(n, m, K, gamma, (S*) x);
+
+extern "C" size_t mxk_phase_bytes(int K) { return (size_t) K * 4 * sizeof(double) + (size_t) K * 8 * sizeof(float); }
+
+extern "C" void mxk_phase_fill(int K, double* h) {
+  float* f = reinterpret_cast<float*>(h + 4 * (size_t) K);
+  for (int q = 0; q < 4 * K; q++) {
+    Sc c = make_sc(h[q]);
+    f[2 * q] = c.hi;
+    f[2 * q + 1] = c.lo;
+  }
+}
+
+extern "C" int mxk_afw_factors(int n, const float* kappa_f, double alpha, double beta, void* out, mx_stream s) {
+  size_t nn = (size_t) n * n;
+  k_afw_factors<<<nblocks(nn), TPB, 0, (cudaStream_t) s>>>(n, kappa_f, (float) (alpha * (double) n * (double) n),
+                                                           (float) (8.0 * beta / 6.0), (float4*) out);
   MX_CHECK_LAUNCH();
   return 0;
 }
 
 extern "C" int mxk_edge_apply(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
                               double beta, const double* beta_kv, double cy, int px, const void* x,
-                              int py, void* y, mx_stream s) {
-  dim3 g(nblocks((size_t) n * n * m * K)), b(TPB);
+                              int py, const void* yin, void* y, mx_stream s) {
+  dim3 g = grd2((size_t) n * n, m, K), b = blk2(m);
   cudaStream_t st = (cudaStream_t) s;
-  if (px == MX_C64 && py == MX_C64)
-    k_edge_apply<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, make_kap<float>(kap, n), alpha, beta, beta_kv, cy, (const float2*) x, (float2*) y);
-  else if (px == MX_C128 && py == MX_C128)
-    k_edge_apply<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, make_kap<double>(kap, n), alpha, beta, beta_kv, cy, (const double2*) x, (double2*) y);
-  else if (px == MX_CDD && py == MX_CDD)
-    k_edge_apply<cdd, cdd, dd><<<g, b, 0, st>>>(n, m, K, ph, make_kap<dd>(kap, n), alpha, beta, beta_kv, cy, (const cdd*) x, (cdd*) y);
-  else if (px == MX_CDD && py == MX_C64)
-    k_edge_apply<cdd, float2, dd><<<g, b, 0, st>>>(n, m, K, ph, make_kap<dd>(kap, n), alpha, beta, beta_kv, cy, (const cdd*) x, (float2*) y);
-  else if (px == MX_C64 && py == MX_CDD)
-    k_edge_apply<float2, cdd, float><<<g, b, 0, st>>>(n, m, K, ph, make_kap<float>(kap, n), alpha, beta, beta_kv, cy, (const float2*) x, (cdd*) y);
-  else
-    return (int) cudaErrorInvalidValue;
+  Sc axy = make_sc(alpha * (double) n * (double) n), mm = make_sc(beta / 6.0), c = make_sc(cy);
+  int has = cy != 0.0;
+#define MX_EA(SX, SY, R)                                                                              \
+  k_edge_apply<SX, SY, R><<<g, b, 0, st>>>(n, m, K, ph, make_kap<R>(kap, n), axy, mm, beta_kv, c, has, \
+                                           (const SX*) x, (const SY*) yin, (SY*) y)
+  if (px == MX_C64 && py == MX_C64) MX_EA(float2, float2, float);
+  else if (px == MX_C128 && py == MX_C128) MX_EA(double2, double2, double);
+  else if (px == MX_CDD && py == MX_CDD) MX_EA(cdd, cdd, dd);
+  else if (px == MX_CDD && py == MX_C64) MX_EA(cdd, float2, dd);
+  else if (px == MX_C64 && py == MX_CDD) MX_EA(float2, cdd, float);
+  else return (int) cudaErrorInvalidValue;
+#undef MX_EA
   MX_CHECK_LAUNCH();
   return 0;
 }
@@ -713,8 +935,8 @@ extern "C" int mxk_edge_restrict(int nc, int m, int K, const double* ph, double 
   return MX_BY_PREC(prec, L_edge_restrict, nc, m, K, ph, alpha, f, c, (cudaStream_t) s);
 }
 extern "C" int mxk_node_apply(int n, int m, int K, const double* ph, double alpha, double cy, int prec,
-                              const void* x, void* y, mx_stream s) {
-  return MX_BY_PREC(prec, L_node_apply, n, m, K, ph, alpha, cy, x, y, (cudaStream_t) s);
+                              const void* x, const void* yin, void* y, mx_stream s) {
+  return MX_BY_PREC(prec, L_node_apply, n, m, K, ph, alpha, cy, x, yin, y, (cudaStream_t) s);
 }
 
 // Node order (node2d.c:629-1138): forward row 0, odd rows 1..n-3, even rows
@@ -752,36 +974,34 @@ extern "C" int mxk_node_restrict(int nc, int m, int K, const double* ph, double 
 
 extern "C" int mxk_gradient(int n, int m, int K, const double* ph, double alpha, int pv, const void* v,
                             int pe, void* e, mx_stream s) {
-  dim3 g(nblocks((size_t) n * n * m * K)), b(TPB);
+  dim3 g = grd2((size_t) n * n, m, K), b = blk2(m);
   cudaStream_t st = (cudaStream_t) s;
-  if (pv == MX_C64 && pe == MX_C64)
-    k_gradient<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, alpha, (const float2*) v, (float2*) e);
-  else if (pv == MX_C128 && pe == MX_C128)
-    k_gradient<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, alpha, (const double2*) v, (double2*) e);
-  else if (pv == MX_C64 && pe == MX_CDD)
-    k_gradient<float2, cdd, dd><<<g, b, 0, st>>>(n, m, K, ph, alpha, (const float2*) v, (cdd*) e);
-  else if (pv == MX_CDD && pe == MX_CDD)
-    k_gradient<cdd, cdd, dd><<<g, b, 0, st>>>(n, m, K, ph, alpha, (const cdd*) v, (cdd*) e);
-  else
-    return (int) cudaErrorInvalidValue;
+  Sc a = make_sc(alpha);
+#define MX_G(SV, SE, R) k_gradient<SV, SE, R><<<g, b, 0, st>>>(n, m, K, ph, a, (const SV*) v, (SE*) e)
+  if (pv == MX_C64 && pe == MX_C64) MX_G(float2, float2, float);
+  else if (pv == MX_C128 && pe == MX_C128) MX_G(double2, double2, double);
+  else if (pv == MX_C64 && pe == MX_CDD) MX_G(float2, cdd, dd);
+  else if (pv == MX_CDD && pe == MX_CDD) MX_G(cdd, cdd, dd);
+  else return (int) cudaErrorInvalidValue;
+#undef MX_G
   MX_CHECK_LAUNCH();
   return 0;
 }
 
 extern "C" int mxk_adjgradient(int n, int m, int K, const double* ph, double alpha, int mass, double cv,
                                int pe, const void* e, int pv, void* v, mx_stream s) {
-  dim3 g(nblocks((size_t) n * n * m * K)), b(TPB);
+  dim3 g = grd2((size_t) n * n, m, K), b = blk2(m);
   cudaStream_t st = (cudaStream_t) s;
-  if (pe == MX_C64 && pv == MX_C64)
-    k_adjgradient<float2, float2, float><<<g, b, 0, st>>>(n, m, K, ph, alpha, mass, cv, (const float2*) e, (float2*) v);
-  else if (pe == MX_C128 && pv == MX_C128)
-    k_adjgradient<double2, double2, double><<<g, b, 0, st>>>(n, m, K, ph, alpha, mass, cv, (const double2*) e, (double2*) v);
-  else if (pe == MX_CDD && pv == MX_C64)
-    k_adjgradient<cdd, float2, dd><<<g, b, 0, st>>>(n, m, K, ph, alpha, mass, cv, (const cdd*) e, (float2*) v);
-  else if (pe == MX_CDD && pv == MX_CDD)
-    k_adjgradient<cdd, cdd, dd><<<g, b, 0, st>>>(n, m, K, ph, alpha, mass, cv, (const cdd*) e, (cdd*) v);
-  else
-    return (int) cudaErrorInvalidValue;
+  Sc a = make_sc(alpha), sixth = make_sc(1.0 / 6.0), c = make_sc(cv);
+  int has = cv != 0.0;
+#define MX_AG(SE, SV, R) \
+  k_adjgradient<SE, SV, R><<<g, b, 0, st>>>(n, m, K, ph, a, mass, sixth, c, has, (const SE*) e, (SV*) v)
+  if (pe == MX_C64 && pv == MX_C64) MX_AG(float2, float2, float);
+  else if (pe == MX_C128 && pv == MX_C128) MX_AG(double2, double2, double);
+  else if (pe == MX_CDD && pv == MX_C64) MX_AG(cdd, float2, dd);
+  else if (pe == MX_CDD && pv == MX_CDD) MX_AG(cdd, cdd, dd);
+  else return (int) cudaErrorInvalidValue;
+#undef MX_AG
   MX_CHECK_LAUNCH();
   return 0;
 }
@@ -812,19 +1032,22 @@ extern "C" int mxk_axpy(double are, double aim, int px, const void* x, int py, v
                         mx_stream s) {
   dim3 g(nblocks(len)), b(TPB);
   cudaStream_t st = (cudaStream_t) s;
-  if (px == MX_C64 && py == MX_C64) k_axpy<float2, float2, float><<<g, b, 0, st>>>(are, aim, (const float2*) x, (float2*) y, len);
-  else if (px == MX_C128 && py == MX_C128) k_axpy<double2, double2, double><<<g, b, 0, st>>>(are, aim, (const double2*) x, (double2*) y, len);
-  else if (px == MX_CDD && py == MX_CDD) k_axpy<cdd, cdd, dd><<<g, b, 0, st>>>(are, aim, (const cdd*) x, (cdd*) y, len);
-  else if (px == MX_C64 && py == MX_CDD) k_axpy<float2, cdd, dd><<<g, b, 0, st>>>(are, aim, (const float2*) x, (cdd*) y, len);
-  else if (px == MX_C64 && py == MX_C128) k_axpy<float2, double2, double><<<g, b, 0, st>>>(are, aim, (const float2*) x, (double2*) y, len);
+  Sc ar = make_sc(are), ai = make_sc(aim);
+#define MX_AX(SX, SY, R) k_axpy<SX, SY, R><<<g, b, 0, st>>>(ar, ai, (const SX*) x, (SY*) y, len)
+  if (px == MX_C64 && py == MX_C64) MX_AX(float2, float2, float);
+  else if (px == MX_C128 && py == MX_C128) MX_AX(double2, double2, double);
+  else if (px == MX_CDD && py == MX_CDD) MX_AX(cdd, cdd, dd);
+  else if (px == MX_C64 && py == MX_CDD) MX_AX(float2, cdd, dd);
+  else if (px == MX_C64 && py == MX_C128) MX_AX(float2, double2, double);
   else return (int) cudaErrorInvalidValue;
+#undef MX_AX
   MX_CHECK_LAUNCH();
   return 0;
 }
 
-extern "C" int mxk_center(int n, int m, int K, const int* gamma, int prec, void* x, mx_stream s) {
+extern "C" int mxk_center(int n, int m, int K, const int* gamma, int prec, void* x, double* acc, mx_stream s) {
   if (m > 32) return (int) cudaErrorInvalidValue;
-  return MX_BY_PREC(prec, L_center, n, m, K, gamma, x, (cudaStream_t) s);
+  return MX_BY_PREC(prec, L_center, n, m, K, gamma, x, acc, (cudaStream_t) s);
 }
 
 extern "C" int mxk_dot(size_t per, int m, int K, int px, const void* x, int py, const void* y, double* out,
