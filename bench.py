@@ -293,6 +293,25 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_kernels(args):
+    """Per-kernel roofline table of one block step's kernels at 512^2 with
+    --nk k-points and block 16 (not the headline metric)."""
+    import maxwell_gb300 as mx
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    rows = mx.kernel_bench(N0 << LEVELS, args.nk, BLOCK, args.reps)
+    for r in rows:
+        gbs = r["bytes"] / (r["ms"] / 1e3) / 1e9
+        print(json.dumps({"kernel": r["name"], "n": N0 << LEVELS, "k_points": args.nk, "block": BLOCK,
+                          "ms_per_call": r["ms"], "launches_per_call": r["launches"],
+                          "algorithmic_bytes": r["bytes"], "achieved_gbs": gbs, "peak_gbs": hbm,
+                          "frac": gbs / hbm}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,8 +319,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead of the metric")
+    ap.add_argument("--nk", type=int, default=NK, help="k-points of the --kernels table")
+    ap.add_argument("--reps", type=int, default=5, help="timed calls per kernel of the --kernels table")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.kernels:
+        run_kernels(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

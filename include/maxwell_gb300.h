@@ -183,6 +183,21 @@ int mxg_eps_sensitivity(int n, const double *kappa, int nk, const mxg_field *xfa
                         const mxg_field *yfactor, int m, const mxg_field *evec,
                         const double *weights, double *grad);
 
+/* ---------- per-kernel timing (no counterpart in the reference) ---------- */
+/* Times each hot kernel of one block step at n x n cells, K k-points and
+ * block m (<= 16) on synthetic blocks: `reps` calls after one untimed call,
+ * CUDA events on the launching stream.  Fills up to maxrows (>= 16) rows with
+ * the mean milliseconds per call, the call's algorithmic bytes (each array
+ * read or written once) and its kernel launches; returns the number of rows,
+ * MXG_EINVAL / MXG_ENOMEM, or -1000 - cudaError_t. */
+typedef struct {
+  char name[40];
+  double ms;
+  double bytes;
+  int launches;
+} mxg_kbench_row;
+int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows);
+
 int mxg_device_ok(void);
 
 #ifdef __cplusplus

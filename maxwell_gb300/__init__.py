@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
             "mxg_solver_kernel_time": (I, [P, P, P, P]),
             "mxg_eps_sensitivity": (I, [I, P, I, P, P, I, P, P, P]),
             "mxg_device_ok": (I, []),
+            "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
         }
         for name, (res, args) in protos.items():
             f = getattr(L, name)
@@ -119,6 +120,21 @@ def _ptr(a: np.ndarray):
 def check(code: int, what: str = "call") -> None:
     if code != 0:
         raise RuntimeError(f"libmaxwell_gb300 {what} failed with status {code}")
+
+
+class KBenchRow(C.Structure):
+    _fields_ = [("name", C.c_char * 40), ("ms", C.c_double), ("bytes", C.c_double), ("launches", C.c_int)]
+
+
+def kernel_bench(n: int, K: int, m: int, reps: int = 5) -> list[dict]:
+    """Per-kernel timing of one block step's hot kernels (mxg_kernel_bench):
+    name, mean ms per call, algorithmic bytes per call, launches per call."""
+    rows = (KBenchRow * 32)()
+    r = lib().mxg_kernel_bench(n, K, m, reps, rows, 32)
+    if r < 0:
+        raise RuntimeError(f"mxg_kernel_bench failed: {r}")
+    return [{"name": rows[i].name.decode(), "ms": rows[i].ms, "bytes": rows[i].bytes,
+             "launches": rows[i].launches} for i in range(r)]
 
 
 def header_functions() -> list[str]:
