@@ -142,3 +142,35 @@ def test_pinvit_single_vector(oracle, golden):
     xg = oracle.vcycle_node(n0, L, xf, yf, 2, 1, 5, bg, np.zeros_like(bg))
     e = oracle.gradient(n, xf, yf, -1.0, xg, e)
     assert rel(e, g["pinvit"]) < 1e-10
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle):
+    """The CPU reference gradient (om_eps_sensitivity on the oracle's own
+    M-normalised eigenvectors) against central differences of the oracle's
+    eigenvalues, step 1e-6 relative on eps of single cells: 1e-5 relative."""
+    n0, L = 8, 1
+    n = n0 << L
+    rng = np.random.default_rng(3)
+    eps = 1.0 + 11.0 * rng.random(n * n)
+    fac = np.array([[np.exp(0.9j), np.exp(0.4j)]])
+
+    def solve(e, vectors=False):
+        st, lam, _, res, vec = oracle.bloch_solve(1.0 / e, fac, n0=n0, L=L, ieigs=6, m=8, method=1, max_nested=60,
+                                                  max_steps=100, tol=1e-11, relative=1, extrapolation="n",
+                                                  wave=1, want_vectors=vectors)
+        assert st == 0 and res[:, :6].max() <= 1e-11
+        return lam, vec
+
+    lam, vec = solve(eps, True)
+    band = 1
+    assert abs(lam[0, band] - lam[0, band - 1]) > 1e-6 and abs(lam[0, band + 1] - lam[0, band]) > 1e-6
+    w = np.zeros(8)
+    w[band] = 1.0
+    g = oracle.eps_sensitivity(n, 1.0 / eps, *fac[0], vec[0], w)
+    for c in (5, 77, 200):
+        h = 1e-6 * eps[c]
+        ep, em = eps.copy(), eps.copy()
+        ep[c] += h
+        em[c] -= h
+        fd = (solve(ep)[0][0, band] - solve(em)[0][0, band]) / (2 * h)
+        assert abs(fd - g[c]) <= 1e-5 * np.abs(g).max(), (c, fd, g[c])
