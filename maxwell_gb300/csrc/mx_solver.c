@@ -21,6 +21,7 @@
 #include "maxwell_gb300.h"
 #include "mx_internal.h"
 
+#include <cuda_profiler_api.h>
 #include <cuda_runtime_api.h>
 #include <math.h>
 #include <stdio.h>
@@ -81,6 +82,7 @@ struct mxg_solver {
   int npev, maxpev;
   double prof_ms;
   long prof_count;
+  int prof_step, prof_done;          /* profiler window (MXG_PROFILE_STEP) */
 };
 
 #define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
@@ -229,6 +231,9 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   s->h_conv = malloc(sizeof(int) * K);
   s->h_steps = malloc(sizeof(int) * K);
   s->timing = getenv("MXG_TIMING") != 0;
+  /* MXG_PROFILE_STEP=q brackets finest-level block step q of the first wave
+   * with cudaProfilerStart/Stop, for a profiler started with profiling off */
+  s->prof_step = getenv("MXG_PROFILE_STEP") ? atoi(getenv("MXG_PROFILE_STEP")) : -1;
   if(s->timing) {
     int q;
     for(q = 0; q <= PH_N; q++) cudaEventCreate(&s->tev[q]);
@@ -522,8 +527,13 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
       if(!s->h_conv[k]) { all = 0; s->h_steps[k] = step + 1; }
     }
     if(all) break;
+    if(l == s->L && step == s->prof_step && !s->prof_done) cudaProfilerStart();
     TRY(block_step(s, l, &have_p));
     TRY(residual(s, l, 1));
+    if(l == s->L && step == s->prof_step && !s->prof_done) {
+      cudaProfilerStop();
+      s->prof_done = 1;
+    }
     if(s->timing && l == s->L && s->o.method == 1) {
       int q;
       cudaEventRecord(s->tev[PH_N], s->st);
