@@ -80,6 +80,21 @@ int add_edge2d_gpu(mxg_field alpha, const edge2d_gpu *x, edge2d_gpu *y);
 /* norms and products per (k, vector): out has K*m entries */
 int norm2_edge2d_gpu(const edge2d_gpu *x, double *out);
 int center_edge2d_gpu(edge2d_gpu *x);
+/* No counterpart in the reference.  center_edge2d_gpu for callers that must
+ * not allocate device memory (an application that owns a fixed device budget
+ * or its own pool, or a loop that cannot take the device synchronisation
+ * cudaMalloc/cudaFree may cause).  x: device batch of K k-points x m vectors
+ * in the device layout [k][2n^2 entries][vector], precision prec; gamma_flag:
+ * K device ints, non-zero for the k-points to centre; stream: a cudaStream_t
+ * (NULL = the legacy default stream) on which the work is enqueued.  The call
+ * allocates nothing: its scratch (4 doubles per k-point and vector) is a
+ * static device array for at most MXG_CENTER_NOALLOC_MAX_KM (k-point, vector)
+ * pairs (256 KiB, held by every GPU that loads the library until exit); a
+ * larger K*m returns MXG_EINVAL.  The first call on a device looks up the
+ * array's address there, so make it before any stream capture.  All calls on
+ * a device share the array: calls that overlap on the GPU race. */
+#define MXG_CENTER_NOALLOC_MAX_KM 8192
+int center_edge2d_gpu_noalloc(int n, int m, int K, const int *gamma_flag, int prec, void *x, void *stream);
 /* y += alpha A x + beta M x (edge2d.c:1335-1650) */
 int addeval_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *x, edge2d_gpu *y);
 /* the same with one beta per (k, vector): the PINVIT defect with its own shift */

@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
             "add_edge2d_gpu": (I, [Field, P, P]),
             "norm2_edge2d_gpu": (I, [P, P]),
             "center_edge2d_gpu": (I, [P]),
+            "center_edge2d_gpu_noalloc": (I, [I, I, I, P, I, P, P]),
             "addeval_edge2d_gpu": (I, [Field, Field, P, P]),
             "addeval_shifted_edge2d_gpu": (I, [D, P, P, P]),
             "energyprod_edge2d_gpu": (I, [Field, Field, P, P, P]),

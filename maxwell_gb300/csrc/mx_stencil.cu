@@ -14,6 +14,9 @@
 // On the unit square with h = 1/n: axy = alpha*n^2, mx = my = beta/6.
 #include "mx_common.cuh"
 #include "mx_internal.h"
+#include "maxwell_gb300.h"
+
+#include <atomic>
 
 using namespace mx;
 
@@ -1048,6 +1051,43 @@ extern "C" int mxk_axpy(double are, double aim, int px, const void* x, int py, v
 extern "C" int mxk_center(int n, int m, int K, const int* gamma, int prec, void* x, double* acc, mx_stream s) {
   if (m > 32) return (int) cudaErrorInvalidValue;
   return MX_BY_PREC(prec, L_center, n, m, K, gamma, x, acc, (cudaStream_t) s);
+}
+
+// ------------------------------------------------------------------
+// center_edge2d_gpu_noalloc: plane centring for callers that must not
+// allocate device memory -- a host application that hands this library a
+// fixed memory budget or its own pool, or a loop that cannot afford the
+// device-wide synchronisation that cudaMalloc/cudaFree may cause.  The
+// kernels are the ones of mxk_center; only their scratch (the plane sums,
+// 4 doubles per k-point and vector) lives in the file-scope array below
+// instead of device memory allocated per call.  Host code cannot use the
+// array's name as a device address, so the first call on each device looks
+// the address up with that device current and keeps it.  Every call on a
+// device shares the array; L_center clears the sums before accumulating.
+// ------------------------------------------------------------------
+namespace {
+__device__ __align__(256) double g_center_sums[4 * MXG_CENTER_NOALLOC_MAX_KM];
+constexpr int kMaxDevices = 64;
+std::atomic<double*> g_center_ptr[kMaxDevices];
+}  // namespace
+
+extern "C" int center_edge2d_gpu_noalloc(int n, int m, int K, const int* gamma_flag, int prec, void* x,
+                                         void* stream) {
+  if (n < 2 || m < 1 || m > 32 || K < 1 || (size_t) K * m > MXG_CENTER_NOALLOC_MAX_KM || !gamma_flag || !x
+      || (prec != MXG_C64 && prec != MXG_C128 && prec != MXG_CDD))
+    return MXG_EINVAL;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int) e;
+  if (dev < 0 || dev >= kMaxDevices) return MXG_EINVAL;
+  double* sums = g_center_ptr[dev].load();
+  if (!sums) {
+    // set-up of this device: the same address whoever gets here first
+    e = cudaGetSymbolAddress((void**) &sums, g_center_sums);
+    if (e != cudaSuccess) return (int) e;
+    g_center_ptr[dev].store(sums);
+  }
+  return mxk_center(n, m, K, gamma_flag, prec, x, sums, (mx_stream) stream);
 }
 
 extern "C" int mxk_dot(size_t per, int m, int K, int px, const void* x, int py, const void* y, double* out,
