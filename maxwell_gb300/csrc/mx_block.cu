@@ -35,23 +35,39 @@ struct EA {
     return w ? ph * v : v;
   }
 };
+// the same for stencils inside the unit cell: no seam test, 32-bit offsets
+template <typename S, typename R>
+struct EAI {
+  const S* base;
+  int n, m;
+  __device__ __forceinline__ cx<R> operator()(int p, int i, int j) const {
+    return Store<S, R>::ld(base + ((p * n + j) * n + i) * m);
+  }
+};
 
 
 template <typename R> struct KapB;
 template <> struct KapB<float> {
   const float* p; int n;
+  __device__ float at(int c) const { return p[c]; }
   __device__ float operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
 };
 template <> struct KapB<double> {
   const double* p; int n;
+  __device__ double at(int c) const { return p[c]; }
   __device__ double operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
 };
 template <> struct KapB<dd> {
   const float* p; int n;
-  __device__ dd operator()(int i, int j) const {
-    float2 v = reinterpret_cast<const float2*>(p)[wrapi(i, n) + wrapi(j, n) * n];
+  __device__ dd at(int c) const {
+    float2 v = reinterpret_cast<const float2*>(p)[c];
     return dd_make(v.x, v.y);
   }
+  __device__ dd operator()(int i, int j) const { return at(wrapi(i, n) + wrapi(j, n) * n); }
+};
+template <typename R> struct KapBI {
+  KapB<R> k;
+  __device__ __forceinline__ R operator()(int i, int j) const { return k.at(i + j * k.n); }
 };
 template <typename R> KapB<R> kapb(mxk_kappa k, int n);
 template <> KapB<float> kapb<float>(mxk_kappa k, int n) { KapB<float> r; r.p = k.f; r.n = n; return r; }
@@ -61,6 +77,23 @@ template <> KapB<dd> kapb<dd>(mxk_kappa k, int n) { KapB<dd> r; r.p = k.dd; r.n 
 template <typename R, typename A>
 __device__ __forceinline__ cx<R> curlc(const A& E, int i, int j) {
   return E(0, i, j) - E(0, i, j + 1) - E(1, i, j) + E(1, i + 1, j);
+}
+
+// s + c += a*b for float-float a = (ah, al), b = (bh, bl), dropping al*bl
+__device__ __forceinline__ void comp_mac(float& s, float& c, float ah, float al, float bh, float bl) {
+  float p = ah * bh;
+  float x = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -p)));
+  float t = s + p;
+  float bp = t - s;
+  c += ((s - (t - bp)) + (p - bp)) + x;
+  s = t;
+}
+// (re, im) += conj(a) * b for float-float complex a, b
+__device__ __forceinline__ void comp_cmac(float* acc, const cx<dd>& a, const cx<dd>& b) {
+  comp_mac(acc[0], acc[1], a.re.hi, a.re.lo, b.re.hi, b.re.lo);
+  comp_mac(acc[0], acc[1], a.im.hi, a.im.lo, b.im.hi, b.im.lo);
+  comp_mac(acc[2], acc[3], a.re.hi, a.re.lo, b.im.hi, b.im.lo);
+  comp_mac(acc[2], acc[3], -a.im.hi, -a.im.lo, b.re.hi, b.re.lo);
 }
 
 // ------------------------------------------------------------------
@@ -90,14 +123,20 @@ __global__ void k_block_residual(int n, int m, int K, const double* __restrict__
   if (row < rows) {
     for (int site = blockIdx.x * rows + row; site < (int) nsite; site += gridDim.x * rows) {
       int i = site % n, j = site / n;
-      cx<R> cc = curlc<R>(E, i, j);
-      cx<R> cb = curlc<R>(E, i, j - 1);
-      cx<R> cl = curlc<R>(E, i - 1, j);
-      cx<R> x0 = E(0, i, j), y0 = E(1, i, j);
-      cx<R> vx = scal(mm, scal(four, x0) + E(0, i, j + 1) + E(0, i, j - 1));
-      cx<R> vy = scal(mm, scal(four, y0) + E(1, i + 1, j) + E(1, i - 1, j));
-      cx<R> wx = scal(axy, scal(kap(i, j), cc) - scal(kap(i, j - 1), cb)) + vx;
-      cx<R> wy = scal(axy, scal(kap(i - 1, j), cl) - scal(kap(i, j), cc)) + vy;
+      cx<R> x0, y0, vx, vy, wx, wy;
+      auto body = [&](const auto& A, const auto& KA) {
+        cx<R> cc = curlc<R>(A, i, j);
+        cx<R> cb = curlc<R>(A, i, j - 1);
+        cx<R> cl = curlc<R>(A, i - 1, j);
+        x0 = A(0, i, j);
+        y0 = A(1, i, j);
+        vx = scal(mm, scal(four, x0) + A(0, i, j + 1) + A(0, i, j - 1));
+        vy = scal(mm, scal(four, y0) + A(1, i + 1, j) + A(1, i - 1, j));
+        wx = scal(axy, scal(KA(i, j), cc) - scal(KA(i, j - 1), cb)) + vx;
+        wy = scal(axy, scal(KA(i - 1, j), cl) - scal(KA(i, j), cc)) + vy;
+      };
+      if (i > 0 && i < n - 1 && j > 0 && j < n - 1) body(EAI<SE, R>{E.base, n, m}, KapBI<R>{kap});
+      else body(E, kap);
       cx<R> rx = wx - scal(muv, vx), ry = wy - scal(muv, vy);
       if (rout) {
         Store<SR, R>::st(rout + L.edge(k, 0, j, i, v), rx);
@@ -448,6 +487,89 @@ __global__ void k_block_combine(CombArgs a, SO* __restrict__ out) {
 }
 
 // ------------------------------------------------------------------
+// Block combination of the mixed solver as a tiled product: a CTA takes
+// tiles of CTE entries (site, plane) of one k-point, loads each source
+// block's tile (CTE x m contiguous values) and the coefficients into shared
+// memory, and every thread forms 4 outputs (entries e0 + 16q, column j).
+// Rows of a float-float source (the eigenvector block) are accumulated as
+// compensated FP32 sums of exact products, the c64 rows in FP32; the
+// float-float output is the normalised sum of both.
+// ------------------------------------------------------------------
+constexpr int CT = 256;       // threads
+constexpr int CTE = 64;       // entries per tile
+
+template <bool DDOUT>
+__global__ void __launch_bounds__(CT) k_block_combine_tiled(CombArgs a, void* out) {
+  const int k = blockIdx.y, m = a.m, nb = a.nb, nsrc = nb * m;
+  __shared__ float4 cS[48 * 16];            // coefficient pairs [row][column]
+  __shared__ float4 tE[CTE * 16];           // float-float source tile
+  __shared__ float2 tF[2][CTE * 16];        // c64 source tiles (at most two)
+  const int tid = threadIdx.x;
+  for (int q = tid; q < nsrc * m; q += CT) {
+    int i = q / m, j = q % m;
+    cS[i * 16 + j] = a.cpair[(size_t) k * a.ldc * m + (size_t) j * a.ldc + a.row0 + i];
+  }
+  const bool dd0 = a.precs[0] == MX_CDD;
+  const int j = tid & 15, e0 = tid >> 4;
+  const bool live = j < m;
+  const size_t per_k = (size_t) 2 * a.n * a.n;           // entries per k-point
+  const size_t ntiles = (per_k + CTE - 1) / CTE;
+  for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const size_t e_start = tile * CTE;
+    const int nte = (int) (per_k - e_start < (size_t) CTE ? per_k - e_start : (size_t) CTE);
+    __syncthreads();
+    for (int b = 0; b < nb; b++) {
+      const size_t off = ((size_t) k * per_k + e_start) * m;
+      const int len = nte * m;
+      if (b == 0 && dd0) {
+        const float4* src = (const float4*) a.ptrs[0] + off;
+        for (int q = tid; q < len; q += CT) tE[q] = src[q];
+      } else {
+        const float2* src = (const float2*) a.ptrs[b] + off;
+        float2* dst = tF[dd0 ? b - 1 : b];
+        for (int q = tid; q < len; q += CT) dst[q] = src[q];
+      }
+    }
+    __syncthreads();
+    if (!live) continue;
+#pragma unroll
+    for (int qq = 0; qq < 4; qq++) {
+      const int e = e0 + 16 * qq;
+      if (e >= nte) break;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};     // compensated sums re (s, c), im (s, c)
+      float fre = 0.f, fim = 0.f;
+      int row = 0;
+      if (dd0) {
+        for (int i = 0; i < m; i++) {
+          float4 c = cS[i * 16 + j], v = tE[e * m + i];
+          comp_mac(acc[0], acc[1], c.x, c.y, v.x, v.y);
+          comp_mac(acc[0], acc[1], -c.z, -c.w, v.z, v.w);
+          comp_mac(acc[2], acc[3], c.x, c.y, v.z, v.w);
+          comp_mac(acc[2], acc[3], c.z, c.w, v.x, v.y);
+        }
+        row = m;
+      }
+      for (int b = dd0 ? 1 : 0; b < nb; b++) {
+        const float2* t = tF[dd0 ? b - 1 : b] + e * m;
+        for (int i = 0; i < m; i++, row++) {
+          float4 c = cS[row * 16 + j];
+          float2 v = t[i];
+          fre = fmaf(c.x, v.x, fmaf(-c.z, v.y, fre));
+          fim = fmaf(c.x, v.y, fmaf(c.z, v.x, fim));
+        }
+      }
+      const size_t o = ((size_t) k * per_k + e_start + e) * m + j;
+      if (DDOUT) {
+        dd re = two_sum(acc[0], acc[1] + fre), im = two_sum(acc[2], acc[3] + fim);
+        reinterpret_cast<float4*>(out)[o] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      } else {
+        reinterpret_cast<float2*>(out)[o] = make_float2(acc[0] + acc[1] + fre, acc[2] + acc[3] + fim);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------
 // sensitivity: grad[c] = -n^2 kappa_c^2 sum_{k,v} w_kv |curl_c e_kv|^2
 // ------------------------------------------------------------------
 template <typename S, typename R>
@@ -503,6 +625,238 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
   return 0;
 }
 
+// ------------------------------------------------------------------
+// Gram matrices of the mixed solver: column block 0 is the float-float
+// eigenvector block E (m <= 16 columns), blocks 1.. are c64, and the
+// entries between a c64 column s_i and an E column e_j take the residual
+// form theta_j s_i^H M e_j + s_i^H r_j.  One CTA of G2T threads takes a chunk
+// of sites of one k-point, in tiles of G2S sites staged in shared memory:
+//   threads 0..255   the FP32 entries: thread (tx, ty) owns the entry
+//                    (bi*m + ty, bj*m + tx) of every block pair bi > bj, so
+//                    its operands are shared along rows and columns, plus a
+//                    share of the lower triangles of the diagonal blocks
+//                    bi = bj >= 1;
+//   threads 256..527 the E-E entries (lower triangle, <= 136), two threads
+//                    per entry on alternate sites of a tile, accumulated as
+//                    compensated FP32 sums of exact products (TwoProd by
+//                    FMA, TwoSum; the low parts of E enter through the
+//                    cross products), which carry about twice the FP32
+//                    precision like float-float arithmetic at half its cost.
+// Partial sums per CTA go to scratch in the layout of k_block_gram.
+// ------------------------------------------------------------------
+constexpr int G2T = 544;         // 17 warps
+constexpr int G2S = 16;          // sites per tile
+constexpr int G2MAXO = 3;        // off-diagonal block pairs (nb <= 3)
+constexpr int G2MAXD = 2;        // diagonal-block entries per FP32 thread
+
+__device__ __forceinline__ void tri_index(int e, int& i, int& j) {
+  i = (int) ((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+  while (i * (i + 1) / 2 > e) i--;
+  while ((i + 1) * (i + 2) / 2 <= e) i++;
+  j = e - i * (i + 1) / 2;
+}
+
+__global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
+  const int k = blockIdx.y, chunk = blockIdx.x;
+  const int n = a.n, m = a.m, ns = a.ns, nb = a.nb;
+  const int nent = ns * (ns + 1) / 2, ment = m * (m + 1) / 2;
+  const int tid = threadIdx.x;
+  extern __shared__ float sm2[];
+  cx<float>* fi = reinterpret_cast<cx<float>*>(sm2);        // [G2S][3][ns]: c, x, y
+  cx<float>* fj = fi + G2S * 3 * ns;                        // [G2S][3][ns]: kappa c, Mx, My
+  cx<float>* fr = fj + G2S * 3 * ns;                        // [G2S][2][m]: rx, ry
+  cx<dd>* di = reinterpret_cast<cx<dd>*>(fr + G2S * 2 * m);  // [G2S][3][m]
+  cx<dd>* dj = di + G2S * 3 * m;                             // [G2S][3][m]
+  Lay L{n, m, a.K};
+  const dd sixth_d = sget<dd>(a.sixth), four_d = rc<dd>(4.0f);
+  const float sixth_f = a.sixth.hi;
+  const bool use_r = a.resid != nullptr;
+
+  // ---- roles ----
+  // block pairs bi > bj in a fixed order; loops over them are unrolled so
+  // that the per-thread entry lists stay in registers
+  constexpr int PBI[G2MAXO] = {1, 2, 2}, PBJ[G2MAXO] = {0, 0, 1};
+  const bool frole = tid < 256;
+  const int tx = tid & 15, ty = (tid >> 4) & 15;
+  const bool otile = frole && tx < m && ty < m;
+  int dli[G2MAXD], dlj[G2MAXD];
+  bool dact[G2MAXD];
+  // accumulators: FP32 threads use all of acc (3 off-diagonal entries, then
+  // 2 diagonal ones, 4 floats each), E-E threads the first 8 (A, M as
+  // compensated sums)
+  float acc[4 * (G2MAXO + G2MAXD)];
+  const int ndiag = (nb - 1) * ment;
+#pragma unroll
+  for (int q = 0; q < G2MAXD; q++) {
+    int e = tid + 256 * q, i = 0, j = 0;
+    dact[q] = frole && e < ndiag;
+    if (dact[q]) tri_index(e % ment, i, j);
+    int blk = dact[q] ? 1 + e / ment : 0;
+    dli[q] = blk * m + i;
+    dlj[q] = blk * m + j;
+  }
+  const int u = tid - 256;
+  const bool drole = u >= 0 && (u >> 1) < ment;
+  const int half = u & 1;
+  int ei = 0, ej = 0;
+  if (drole) tri_index(u >> 1, ei, ej);
+#pragma unroll
+  for (int q = 0; q < 4 * (G2MAXO + G2MAXD); q++) acc[q] = 0.f;
+  float* const eacc_a = acc;
+  float* const eacc_m = acc + 4;
+
+  const size_t nsite = (size_t) n * n;
+  const size_t per = (nsite + a.chunks - 1) / a.chunks;
+  const size_t s0 = (size_t) chunk * per, s1 = s0 + per < nsite ? s0 + per : nsite;
+  for (size_t base = s0; base < s1; base += G2S) {
+    const int nts = (int) (s1 - base < (size_t) G2S ? s1 - base : (size_t) G2S);
+    __syncthreads();
+    // ---- staging ----
+    for (int w = tid; w < G2S * ns; w += G2T) {
+      int ts = w / ns, col = w % ns;
+      if (ts >= nts) continue;
+      size_t site = base + ts;
+      int i = (int) (site % n), j = (int) (site / n);
+      int b = col / m, v = col % m;
+      size_t o0 = L.edge(k, 0, 0, 0, v);
+      bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
+      cx<float>* fI = fi + ts * 3 * ns + col;
+      cx<float>* fJ = fj + ts * 3 * ns + col;
+      if (b == 0) {
+        // E column: float-float values, and their leading floats for the FP32 entries
+        const cdd* eb = (const cdd*) a.ptrs[0] + o0;
+        cx<dd>* dI = di + ts * 3 * m + v;
+        cx<dd>* dJ = dj + ts * 3 * m + v;
+        const dd kap = dd_make(a.kap.dd[2 * site], a.kap.dd[2 * site + 1]);
+        auto body = [&](const auto& E) {
+          cx<dd> x0 = E(0, i, j), t = E(0, i, j + 1);
+          dI[m] = x0;
+          fI[ns] = mkc(x0.re.hi, x0.im.hi);
+          cx<dd> mx = scal(sixth_d, scal(four_d, x0) + t + E(0, i, j - 1));
+          dJ[m] = mx;
+          fJ[ns] = mkc(mx.re.hi, mx.im.hi);
+          cx<dd> c = x0 - t;
+          cx<dd> y0 = E(1, i, j), r = E(1, i + 1, j);
+          dI[2 * m] = y0;
+          fI[2 * ns] = mkc(y0.re.hi, y0.im.hi);
+          cx<dd> my = scal(sixth_d, scal(four_d, y0) + r + E(1, i - 1, j));
+          dJ[2 * m] = my;
+          fJ[2 * ns] = mkc(my.re.hi, my.im.hi);
+          c = c - y0 + r;
+          dI[0] = c;
+          fI[0] = mkc(c.re.hi, c.im.hi);
+          cx<dd> kc = scal(kap, c);
+          dJ[0] = kc;
+          fJ[0] = mkc(kc.re.hi, kc.im.hi);
+        };
+        if (inner) body(EAI<cdd, dd>{eb, n, m});
+        else body(EA<cdd, dd>{eb, n, m, seam_load<dd>(a.ph, a.K, k, n)});
+      } else {
+        const float2* xb = (const float2*) a.ptrs[b] + o0;
+        const float kap = a.kap.f[site];
+        auto body = [&](const auto& X) {
+          cx<float> x0 = X(0, i, j), t = X(0, i, j + 1), y0 = X(1, i, j), r = X(1, i + 1, j);
+          cx<float> c = x0 - t - y0 + r;
+          fI[0] = c; fI[ns] = x0; fI[2 * ns] = y0;
+          fJ[0] = scal(kap, c);
+          fJ[ns] = scal(sixth_f, scal(4.0f, x0) + t + X(0, i, j - 1));
+          fJ[2 * ns] = scal(sixth_f, scal(4.0f, y0) + r + X(1, i - 1, j));
+        };
+        if (inner) body(EAI<float2, float>{xb, n, m});
+        else body(EA<float2, float>{xb, n, m, seam_load<float>(a.ph, a.K, k, n)});
+      }
+    }
+    if (use_r)
+      for (int w = tid; w < G2S * m; w += G2T) {
+        int ts = w / m, v = w % m;
+        if (ts >= nts) continue;
+        size_t site = base + ts;
+        int i = (int) (site % n), j = (int) (site / n);
+        float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
+        fr[ts * 2 * m + v] = mkc(rx.x, rx.y);
+        fr[ts * 2 * m + m + v] = mkc(ry.x, ry.y);
+      }
+    __syncthreads();
+    // ---- accumulation ----
+    if (frole) {
+      for (int ts = 0; ts < nts; ts++) {
+        const cx<float>* I = fi + ts * 3 * ns;
+        const cx<float>* J = fj + ts * 3 * ns;
+        const cx<float>* Rr = fr + ts * 2 * m;
+#pragma unroll
+        for (int q = 0; q < G2MAXO; q++) {
+          if (!otile || PBI[q] >= nb) continue;
+          int i = PBI[q] * m + ty, j = PBJ[q] * m + tx;
+          cx<float> xi = I[ns + i], yi = I[2 * ns + i];
+          cx<float> mm = conjc(xi) * J[ns + j] + conjc(yi) * J[2 * ns + j];
+          cx<float> aa = j < m && use_r ? conjc(xi) * Rr[j] + conjc(yi) * Rr[m + j] : conjc(I[i]) * J[j];
+          acc[4 * q] += aa.re; acc[4 * q + 1] += aa.im; acc[4 * q + 2] += mm.re; acc[4 * q + 3] += mm.im;
+        }
+#pragma unroll
+        for (int q = 0; q < G2MAXD; q++) {
+          if (!dact[q]) continue;
+          int i = dli[q], j = dlj[q];
+          cx<float> mm = conjc(I[ns + i]) * J[ns + j] + conjc(I[2 * ns + i]) * J[2 * ns + j];
+          cx<float> aa = conjc(I[i]) * J[j];
+          float* d = acc + 4 * (G2MAXO + q);
+          d[0] += aa.re; d[1] += aa.im; d[2] += mm.re; d[3] += mm.im;
+        }
+      }
+    } else if (drole) {
+      for (int ts = half; ts < nts; ts += 2) {
+        const cx<dd>* I = di + ts * 3 * m;
+        const cx<dd>* J = dj + ts * 3 * m;
+        comp_cmac(eacc_a, I[ei], J[ej]);
+        comp_cmac(eacc_m, I[m + ei], J[m + ej]);
+        comp_cmac(eacc_m, I[2 * m + ei], J[2 * m + ej]);
+      }
+    }
+  }
+  // ---- partial sums of this CTA ----
+  __syncthreads();
+  double axy = (double) n * (double) n;
+  double* out = a.partial + (((size_t) k * a.chunks + chunk) * nent) * 4;
+  auto put = [&](int i, int j, double ar, double ai, double mr, double mi) {
+    int e = i * (i + 1) / 2 + j;
+    if (use_r && i >= m && j < m) {
+      double th = a.theta[(size_t) k * m + j];
+      out[(size_t) e * 4 + 0] = th * mr + ar;
+      out[(size_t) e * 4 + 1] = th * mi + ai;
+    } else {
+      out[(size_t) e * 4 + 0] = axy * ar + mr;
+      out[(size_t) e * 4 + 1] = axy * ai + mi;
+    }
+    out[(size_t) e * 4 + 2] = mr;
+    out[(size_t) e * 4 + 3] = mi;
+  };
+#pragma unroll
+  for (int q = 0; q < G2MAXO; q++)
+    if (otile && PBI[q] < nb) put(PBI[q] * m + ty, PBJ[q] * m + tx, acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+#pragma unroll
+  for (int q = 0; q < G2MAXD; q++)
+    if (dact[q]) put(dli[q], dlj[q], acc[4 * (G2MAXO + q)], acc[4 * (G2MAXO + q) + 1], acc[4 * (G2MAXO + q) + 2],
+                     acc[4 * (G2MAXO + q) + 3]);
+  // the two halves of every E-E entry meet in shared memory
+  double* xch = reinterpret_cast<double*>(sm2);     // [ment][4]
+  if (drole && half == 1) {
+    double* q = xch + (size_t) (u >> 1) * 4;
+    q[0] = (double) eacc_a[0] + (double) eacc_a[1];
+    q[1] = (double) eacc_a[2] + (double) eacc_a[3];
+    q[2] = (double) eacc_m[0] + (double) eacc_m[1];
+    q[3] = (double) eacc_m[2] + (double) eacc_m[3];
+  }
+  __syncthreads();
+  if (drole && half == 0) {
+    const double* q = xch + (size_t) (u >> 1) * 4;
+    put(ei, ej, (double) eacc_a[0] + (double) eacc_a[1] + q[0], (double) eacc_a[2] + (double) eacc_a[3] + q[1],
+        (double) eacc_m[0] + (double) eacc_m[1] + q[2], (double) eacc_m[2] + (double) eacc_m[3] + q[3]);
+  }
+}
+
+static size_t gram_mixed_smem(int ns, int m) {
+  return sizeof(cx<float>) * G2S * (6 * ns + 2 * m) + sizeof(cx<dd>) * G2S * 6 * m;
+}
+
 static int gram_chunks(int K, size_t nsite) {
   int c = (4 * 152 + K - 1) / K;
   if (c < 8) c = 8;
@@ -545,7 +899,13 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
   if (resid && (all128 || mh == 0)) return (int) cudaErrorInvalidValue;
   size_t smem = hsz * TS * mh * 5 + sizeof(cx<float>) * TS * a.ns * 5 + (hsz / 2 + sizeof(float)) * TS
                 + sizeof(cx<float>) * TS * mh * 2 + 16;
-  if (hi_dd) {
+  bool lo_rest = true;
+  for (int q = 1; q < nb; q++) lo_rest = lo_rest && precs[q] == MX_C64;
+  if (hi_dd && lo_rest && m <= 16 && nb <= 3 && (nb == 1 || resid)) {
+    size_t sm = gram_mixed_smem(a.ns, m);
+    cudaFuncSetAttribute(k_block_gram_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    k_block_gram_mixed<<<g, G2T, sm, st>>>(a);
+  } else if (hi_dd) {
     cudaFuncSetAttribute(k_block_gram<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     k_block_gram<dd><<<g, GT, smem, st>>>(a, mh);
   } else {
@@ -573,9 +933,22 @@ extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, 
     a.precs[b] = b < nb ? precs[b] : MX_C64;
     a.ptrs[b] = b < nb ? ptrs[b] : nullptr;
   }
+  cudaStream_t st = (cudaStream_t) s;
+  bool rest64 = true;
+  for (int q = 1; q < nb; q++) rest64 = rest64 && precs[q] == MX_C64;
+  bool first_ok = precs[0] == MX_CDD || precs[0] == MX_C64;
+  int nfloat = precs[0] == MX_CDD ? nb - 1 : nb;
+  if (m <= 16 && nfloat <= 2 && first_ok && rest64 && (pout == MX_CDD || (pout == MX_C64 && precs[0] == MX_C64))) {
+    size_t ntiles = (2 * (size_t) n * n + CTE - 1) / CTE;
+    unsigned gx = (unsigned) (ntiles < 64 ? ntiles : 64);
+    dim3 g2(gx, K);
+    if (pout == MX_CDD) k_block_combine_tiled<true><<<g2, CT, 0, st>>>(a, out);
+    else k_block_combine_tiled<false><<<g2, CT, 0, st>>>(a, out);
+    MX_CHECK_LAUNCH();
+    return 0;
+  }
   unsigned rows = 256 / m;
   dim3 g((unsigned) ((2 * (size_t) n * n + rows - 1) / rows), K), b(m, rows);
-  cudaStream_t st = (cudaStream_t) s;
   size_t ncoef = (size_t) nb * m * m;
   if (pout == MX_CDD)
     k_block_combine<cdd, dd><<<g, b, ncoef * (sizeof(cx<dd>) + sizeof(cx<float>)), st>>>(a, (cdd*) out);

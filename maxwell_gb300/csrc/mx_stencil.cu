@@ -41,18 +41,26 @@ inline unsigned nblocks(size_t work, int tpb = TPB) {
 template <typename R> struct Kap;
 template <> struct Kap<float> {
   const float* p; int n;
+  __device__ float at(int c) const { return p[c]; }
   __device__ float operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
 };
 template <> struct Kap<double> {
   const double* p; int n;
+  __device__ double at(int c) const { return p[c]; }
   __device__ double operator()(int i, int j) const { return p[wrapi(i, n) + wrapi(j, n) * n]; }
 };
 template <> struct Kap<dd> {
   const float* p; int n;
-  __device__ dd operator()(int i, int j) const {
-    float2 v = reinterpret_cast<const float2*>(p)[wrapi(i, n) + wrapi(j, n) * n];
+  __device__ dd at(int c) const {
+    float2 v = reinterpret_cast<const float2*>(p)[c];
     return dd_make(v.x, v.y);
   }
+  __device__ dd operator()(int i, int j) const { return at(wrapi(i, n) + wrapi(j, n) * n); }
+};
+// kappa of a cell known to lie inside [0,n)^2: no wrap
+template <typename R> struct KapI {
+  Kap<R> k;
+  __device__ __forceinline__ R operator()(int i, int j) const { return k.at(i + j * k.n); }
 };
 template <typename R> Kap<R> make_kap(mxk_kappa k, int n);
 template <> Kap<float> make_kap<float>(mxk_kappa k, int n) { Kap<float> r; r.p = k.f; r.n = n; return r; }
@@ -86,6 +94,26 @@ struct NAcc {
   }
 };
 
+// The same two accessors for sites whose whole stencil lies inside the unit
+// cell: no seam test and 32-bit offsets (2n^2 m < 2^31 for every level).  The
+// site kernels take this path for all but the boundary rows and columns.
+template <typename S, typename R>
+struct EAccI {
+  const S* base;
+  int n, m;
+  __device__ __forceinline__ cx<R> operator()(int p, int i, int j) const {
+    return Store<S, R>::ld(base + ((p * n + j) * n + i) * m);
+  }
+};
+template <typename S, typename R>
+struct NAccI {
+  const S* base;
+  int n, m;
+  __device__ __forceinline__ cx<R> operator()(int i, int j) const {
+    return Store<S, R>::ld(base + (j * n + i) * m);
+  }
+};
+
 
 // curl of cell (i,j): bottom - top - left + right
 template <typename R, typename A>
@@ -94,15 +122,15 @@ __device__ __forceinline__ cx<R> curl(const A& E, int i, int j) {
 }
 
 // (alpha A + beta M) x at x-edge (i,j) and y-edge (i,j)
-template <typename R, typename A>
-__device__ __forceinline__ cx<R> kx_x(const A& E, const Kap<R>& kap, R axy, R mm, int i, int j) {
+template <typename R, typename A, typename KA>
+__device__ __forceinline__ cx<R> kx_x(const A& E, const KA& kap, R axy, R mm, int i, int j) {
   cx<R> c0 = E(0, i, j);
   cx<R> mass = scal(mm, scal(rc<R>(4.0f), c0) + E(0, i, j + 1) + E(0, i, j - 1));
   cx<R> cur = scal(kap(i, j), curl<R>(E, i, j)) - scal(kap(i, j - 1), curl<R>(E, i, j - 1));
   return scal(axy, cur) + mass;
 }
-template <typename R, typename A>
-__device__ __forceinline__ cx<R> kx_y(const A& E, const Kap<R>& kap, R axy, R mm, int i, int j) {
+template <typename R, typename A, typename KA>
+__device__ __forceinline__ cx<R> kx_y(const A& E, const KA& kap, R axy, R mm, int i, int j) {
   cx<R> c0 = E(1, i, j);
   cx<R> mass = scal(mm, scal(rc<R>(4.0f), c0) + E(1, i + 1, j) + E(1, i - 1, j));
   cx<R> cur = scal(kap(i - 1, j), curl<R>(E, i - 1, j)) - scal(kap(i, j), curl<R>(E, i, j));
@@ -135,11 +163,20 @@ __global__ void k_edge_apply(int n, int m, int K, const double* __restrict__ ph,
   if (site >= n * n) return;
   int i = site % n, j = site / n;
   Lay L{n, m, K};
-  EAcc<SX, R> E{x + L.edge(k, 0, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
   R axy = sget<R>(axy_s);
   R mm = beta_kv ? Real<R>::from(beta_kv[(size_t) k * m + v] / 6.0) : sget<R>(mm_s);
-  cx<R> ox = kx_x<R>(E, kap, axy, mm, i, j);
-  cx<R> oy = kx_y<R>(E, kap, axy, mm, i, j);
+  const SX* xb = x + L.edge(k, 0, 0, 0, v);
+  cx<R> ox, oy;
+  if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+    EAccI<SX, R> E{xb, n, m};
+    KapI<R> ki{kap};
+    ox = kx_x<R>(E, ki, axy, mm, i, j);
+    oy = kx_y<R>(E, ki, axy, mm, i, j);
+  } else {
+    EAcc<SX, R> E{xb, n, m, seam_load<R>(ph, K, k, n)};
+    ox = kx_x<R>(E, kap, axy, mm, i, j);
+    oy = kx_y<R>(E, kap, axy, mm, i, j);
+  }
   size_t ox_at = L.edge(k, 0, j, i, v), oy_at = L.edge(k, 1, j, i, v);
   if (has_cy) {
     const SY* src = yin ? yin : y;
@@ -159,36 +196,42 @@ __global__ void k_edge_apply(int n, int m, int K, const double* __restrict__ ph,
 // Local matrix T and its factorisation: see patch_solve in the oracle; the
 // reference's starsolve_common (edge2d.c:2029-2183).
 // ------------------------------------------------------------------
-template <typename S, typename R>
-__device__ __forceinline__ void deposit_e(S* base, int n, int m, const Seam<R>& seam, int p, int i,
-                                          int j, cx<R> val) {
-  cx<R> ph;
-  bool w = seam.wrap(i, j, ph);
-  if (w) val = conjc(ph) * val;
-  S* q = base + ((size_t) (p * n + j) * n + i) * m;
-  Store<S, R>::st(q, Store<S, R>::ld(q) + val);
-}
 
-// One (k, vector) edge vector with seam phases on load and store: a value
-// addressed one period outside is the stored value times the phase, and is
-// written back multiplied by the conjugate phase.
+// One row of one plane of a (k, vector) edge vector: the row index is
+// wrapped once (with its seam phase) when the accessor is made, so a load or
+// store tests only the column, which is the same for every thread of a warp
+// in the row sweeps below.
 template <typename S, typename R>
-struct EIO {
-  S* base;
+struct RowIO {
+  S* row;          // column 0 of the stored row
   int n, m;
-  Seam<R> seam;
-  __device__ __forceinline__ cx<R> ld(int p, int i, int j) const {
-    cx<R> ph;
-    bool w = seam.wrap(i, j, ph);
-    cx<R> v = Store<S, R>::ld(base + ((size_t) (p * n + j) * n + i) * m);
-    return w ? ph * v : v;
+  bool rw;         // the addressed row lies one period outside
+  cx<R> rph;       // its phase
+  cx<R> xf;
+  __device__ __forceinline__ cx<R> ld(int i) const {
+    cx<R> v;
+    if (i < 0) v = conjc(xf) * Store<S, R>::ld(row + (i + n) * m);
+    else if (i >= n) v = xf * Store<S, R>::ld(row + (i - n) * m);
+    else v = Store<S, R>::ld(row + i * m);
+    return rw ? rph * v : v;
   }
-  __device__ __forceinline__ void st(int p, int i, int j, cx<R> v) const {
-    cx<R> ph;
-    if (seam.wrap(i, j, ph)) v = conjc(ph) * v;
-    Store<S, R>::st(base + ((size_t) (p * n + j) * n + i) * m, v);
+  __device__ __forceinline__ void st(int i, cx<R> v) const {
+    if (rw) v = conjc(rph) * v;
+    if (i < 0) Store<S, R>::st(row + (i + n) * m, xf * v);
+    else if (i >= n) Store<S, R>::st(row + (i - n) * m, conjc(xf) * v);
+    else Store<S, R>::st(row + i * m, v);
   }
 };
+template <typename S, typename R>
+__device__ __forceinline__ RowIO<S, R> row_io(S* base, int p, int j, int n, int m, const Seam<R>& seam) {
+  RowIO<S, R> r;
+  r.n = n; r.m = m; r.xf = seam.xf;
+  r.rw = j < 0 || j >= n;
+  r.rph = j < 0 ? conjc(seam.yf) : seam.yf;
+  int jj = j < 0 ? j + n : (j >= n ? j - n : j);
+  r.row = base + (p * n + jj) * n * m;
+  return r;
+}
 
 // Sliding window over a row: the thread holds the patch data of vertex
 // (i,j) -- the reference's mxx[2][3], mxy[3][2], meps[2][2], mbx[2], mby[2]
@@ -244,8 +287,12 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
   int j = j0 + (r / m) * jstep;
   Lay L{n, m, K};
   Seam<R> seam = seam_load<R>(ph, K, k, n);
-  EIO<S, R> X{x + L.edge(k, 0, 0, 0, v), n, m, seam};
-  EIO<S, R> B{const_cast<S*>(b) + L.edge(k, 0, 0, 0, v), n, m, seam};
+  S* xk = x + L.edge(k, 0, 0, 0, v);
+  S* bk = const_cast<S*>(b) + L.edge(k, 0, 0, 0, v);
+  const RowIO<S, R> X0m = row_io<S, R>(xk, 0, j - 1, n, m, seam), X0c = row_io<S, R>(xk, 0, j, n, m, seam),
+                    X0p = row_io<S, R>(xk, 0, j + 1, n, m, seam), X1m = row_io<S, R>(xk, 1, j - 1, n, m, seam),
+                    X1c = row_io<S, R>(xk, 1, j, n, m, seam), B0c = row_io<S, R>(bk, 0, j, n, m, seam),
+                    B1m = row_io<S, R>(bk, 1, j - 1, n, m, seam), B1c = row_io<S, R>(bk, 1, j, n, m, seam);
   const R axy = sget<R>(axy_s);
   const R mm = sget<R>(mm_s);
   const R s8 = sget<R>(s8_s);     // 4 (mx + my), mx = my
@@ -254,13 +301,13 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
   const bool tab = ftab != nullptr;
   int i = backward ? n - 1 : 0;
   // x columns i-1 (a) and i (b), rows j-1, j, j+1; y columns i-1 (a), i (b), i+1 (c), rows j-1, j
-  cx<R> xa0 = X.ld(0, i - 1, j - 1), xa1 = X.ld(0, i - 1, j), xa2 = X.ld(0, i - 1, j + 1);
-  cx<R> xb0 = X.ld(0, i, j - 1), xb1 = X.ld(0, i, j), xb2 = X.ld(0, i, j + 1);
-  cx<R> ya0 = X.ld(1, i - 1, j - 1), ya1 = X.ld(1, i - 1, j);
-  cx<R> yb0 = X.ld(1, i, j - 1), yb1 = X.ld(1, i, j);
-  cx<R> yc0 = X.ld(1, i + 1, j - 1), yc1 = X.ld(1, i + 1, j);
+  cx<R> xa0 = X0m.ld(i - 1), xa1 = X0c.ld(i - 1), xa2 = X0p.ld(i - 1);
+  cx<R> xb0 = X0m.ld(i), xb1 = X0c.ld(i), xb2 = X0p.ld(i);
+  cx<R> ya0 = X1m.ld(i - 1), ya1 = X1c.ld(i - 1);
+  cx<R> yb0 = X1m.ld(i), yb1 = X1c.ld(i);
+  cx<R> yc0 = X1m.ld(i + 1), yc1 = X1c.ld(i + 1);
   R kLL = kap(i - 1, j - 1), kUL = kap(i - 1, j), kLR = kap(i, j - 1), kUR = kap(i, j);
-  cx<R> bx0 = B.ld(0, i - 1, j), bx1 = B.ld(0, i, j), by0 = B.ld(1, i, j - 1), by1 = B.ld(1, i, j);
+  cx<R> bx0 = B0c.ld(i - 1), bx1 = B0c.ld(i), by0 = B1m.ld(i), by1 = B1c.ld(i);
   float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fb = fa;
   if (tab) { fa = ftab[2 * ((size_t) j * n + i)]; fb = ftab[2 * ((size_t) j * n + i) + 1]; }
   for (int step = 0; step < n; step++) {
@@ -273,15 +320,15 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
       int ix = backward ? i - 2 : i + 1;    // new x column
       int iy = backward ? i - 2 : i + 2;    // new y column
       int ib = backward ? i - 1 : i + 1;    // new patch column
-      nx0 = X.ld(0, ix, j - 1); nx1 = X.ld(0, ix, j); nx2 = X.ld(0, ix, j + 1);
-      ny0 = X.ld(1, iy, j - 1); ny1 = X.ld(1, iy, j);
+      nx0 = X0m.ld(ix); nx1 = X0c.ld(ix); nx2 = X0p.ld(ix);
+      ny0 = X1m.ld(iy); ny1 = X1c.ld(iy);
       nk0 = kap(ix, j - 1); nk1 = kap(ix, j);
       if (tab) {
         nfa = ftab[2 * ((size_t) j * n + ib)];
         nfb = ftab[2 * ((size_t) j * n + ib) + 1];
       }
-      nbx = B.ld(0, backward ? i - 2 : i + 1, j);
-      nby0 = B.ld(1, ib, j - 1); nby1 = B.ld(1, ib, j);
+      nbx = B0c.ld(backward ? i - 2 : i + 1);
+      nby0 = B1m.ld(ib); nby1 = B1c.ld(ib);
     }
     // residual b - (alpha A + beta M) x at the patch unknowns u0..u3 =
     // x(i-1,j), x(i,j), y(i,j-1), y(i,j) from the four cell curls
@@ -317,12 +364,12 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
     xb1 += scal(quarter, c0 + c1 - c2 - c3);
     yb0 += scal(quarter, c0 - c1 - c2 + c3);
     yb1 += scal(quarter, c0 - c1 + c2 - c3);
-    X.st(1, i, j - 1, yb0);
-    X.st(1, i, j, yb1);
+    X1m.st(i, yb0);
+    X1c.st(i, yb1);
     if (!backward) {
-      X.st(0, i - 1, j, xa1);
+      X0c.st(i - 1, xa1);
       if (last) {
-        X.st(0, i, j, xb1);
+        X0c.st(i, xb1);
         break;
       }
       xa0 = xb0; xa1 = xb1; xa2 = xb2;
@@ -334,9 +381,9 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
       bx0 = bx1; bx1 = nbx; by0 = nby0; by1 = nby1;
       i++;
     } else {
-      X.st(0, i, j, xb1);
+      X0c.st(i, xb1);
       if (last) {
-        X.st(0, i - 1, j, xa1);
+        X0c.st(i - 1, xa1);
         break;
       }
       xb0 = xa0; xb1 = xa1; xb2 = xa2;
@@ -364,11 +411,16 @@ __global__ void k_edge_prolong(int nc, int m, int K, const double* __restrict__ 
   if (site >= nf * nf) return;
   int i = site % nf, j = site / nf;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  EAcc<S, R> C{c + Lc.edge(k, 0, 0, 0, v), nc, m, seam_load<R>(ph, K, k, nc)};
+  const S* cb = c + Lc.edge(k, 0, 0, 0, v);
   int ci = i >> 1, cj = j >> 1;
   R half = rc<R>(0.5f), quarter = rc<R>(0.25f), a = sget<R>(alpha);
-  cx<R> vx = (j & 1) ? scal(quarter, C(0, ci, cj) + C(0, ci, cj + 1)) : scal(half, C(0, ci, cj));
-  cx<R> vy = (i & 1) ? scal(quarter, C(1, ci, cj) + C(1, ci + 1, cj)) : scal(half, C(1, ci, cj));
+  cx<R> vx, vy;
+  auto body = [&](const auto& C) {
+    vx = (j & 1) ? scal(quarter, C(0, ci, cj) + C(0, ci, cj + 1)) : scal(half, C(0, ci, cj));
+    vy = (i & 1) ? scal(quarter, C(1, ci, cj) + C(1, ci + 1, cj)) : scal(half, C(1, ci, cj));
+  };
+  if (ci < nc - 1 && cj < nc - 1) body(EAccI<S, R>{cb, nc, m});
+  else body(EAcc<S, R>{cb, nc, m, seam_load<R>(ph, K, k, nc)});
   S* px = f + Lf.edge(k, 0, j, i, v);
   S* py = f + Lf.edge(k, 1, j, i, v);
   Store<S, R>::st(px, Store<S, R>::ld(px) + scal(a, vx));
@@ -385,13 +437,18 @@ __global__ void k_edge_restrict(int nc, int m, int K, const double* __restrict__
   if (site >= nc * nc) return;
   int i = site % nc, j = site / nc;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  EAcc<S, R> F{f + Lf.edge(k, 0, 0, 0, v), nf, m, seam_load<R>(ph, K, k, nf)};
+  const S* fb = f + Lf.edge(k, 0, 0, 0, v);
   R half = rc<R>(0.5f), quarter = rc<R>(0.25f), a = sget<R>(alpha);
   int fi = 2 * i, fj = 2 * j;
-  cx<R> sx = scal(half, F(0, fi, fj) + F(0, fi + 1, fj))
-             + scal(quarter, F(0, fi, fj - 1) + F(0, fi + 1, fj - 1) + F(0, fi, fj + 1) + F(0, fi + 1, fj + 1));
-  cx<R> sy = scal(half, F(1, fi, fj) + F(1, fi, fj + 1))
-             + scal(quarter, F(1, fi - 1, fj) + F(1, fi - 1, fj + 1) + F(1, fi + 1, fj) + F(1, fi + 1, fj + 1));
+  cx<R> sx, sy;
+  auto body = [&](const auto& F) {
+    sx = scal(half, F(0, fi, fj) + F(0, fi + 1, fj))
+         + scal(quarter, F(0, fi, fj - 1) + F(0, fi + 1, fj - 1) + F(0, fi, fj + 1) + F(0, fi + 1, fj + 1));
+    sy = scal(half, F(1, fi, fj) + F(1, fi, fj + 1))
+         + scal(quarter, F(1, fi - 1, fj) + F(1, fi - 1, fj + 1) + F(1, fi + 1, fj) + F(1, fi + 1, fj + 1));
+  };
+  if (i > 0 && j > 0) body(EAccI<S, R>{fb, nf, m});
+  else body(EAcc<S, R>{fb, nf, m, seam_load<R>(ph, K, k, nf)});
   S* px = c + Lc.edge(k, 0, j, i, v);
   S* py = c + Lc.edge(k, 1, j, i, v);
   Store<S, R>::st(px, Store<S, R>::ld(px) + scal(a, sx));
@@ -416,8 +473,11 @@ __global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph,
   if (site >= n * n) return;
   int i = site % n, j = site / n;
   Lay L{n, m, K};
-  NAcc<S, R> V{x + L.node(k, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
-  cx<R> o = scal(sget<R>(diag), V(i, j)) + scal(sget<R>(off), lap_off<R>(V, i, j));
+  const S* xb = x + L.node(k, 0, 0, v);
+  cx<R> o;
+  auto body = [&](const auto& V) { o = scal(sget<R>(diag), V(i, j)) + scal(sget<R>(off), lap_off<R>(V, i, j)); };
+  if (i > 0 && i < n - 1 && j > 0 && j < n - 1) body(NAccI<S, R>{xb, n, m});
+  else body(NAcc<S, R>{xb, n, m, seam_load<R>(ph, K, k, n)});
   size_t at = L.node(k, j, i, v);
   if (has_cy) o += scal(sget<R>(cy), Store<S, R>::ld((yin ? yin : y) + at));
   Store<S, R>::st(y + at, o);
@@ -456,7 +516,7 @@ struct NIO {
 // time, behind every position pass 1 still reads), pass 2 writes the
 // truncated prefix sums into x.  The new x_{i0} that the last position
 // needs is formed from old values before anything is written.
-constexpr int NSEG = 64, NRING = 88;
+constexpr int NSEG = 64, NRING = 128;   // ring: a power of two >= NSEG + D
 
 template <typename S, typename R, int D>
 __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s,
@@ -479,6 +539,24 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
                + X(ii + 1, j + 1);
     return scal(inv_ac, Store<S, R>::ld(bb + ((size_t) j * n + ii) * m) + scal(third, nb));
   };
+  // positions 1..n-2 of the row: the rows j-1, j+1 through plain pointers,
+  // with the seam phase of the whole row when it lies across the seam
+  const S* xk = x + L.node(k, 0, 0, v);
+  const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+  const S* rowm = xk + jm * n * m;
+  const S* rowp = xk + jp * n * m;
+  const S* rowc = xk + j * n * m;
+  const S* rowb = bb + j * n * m;
+  auto beta_inner = [&](int ii) {
+    cx<R> sm = Store<S, R>::ld(rowm + (ii - 1) * m) + Store<S, R>::ld(rowm + ii * m)
+               + Store<S, R>::ld(rowm + (ii + 1) * m);
+    cx<R> sp = Store<S, R>::ld(rowp + (ii - 1) * m) + Store<S, R>::ld(rowp + ii * m)
+               + Store<S, R>::ld(rowp + (ii + 1) * m);
+    if (j == 0) sm = conjc(seam.yf) * sm;
+    if (j == n - 1) sp = seam.yf * sp;
+    cx<R> nb = Store<S, R>::ld(rowc + (ii + sd) * m) + sm + sp;
+    return scal(inv_ac, Store<S, R>::ld(rowb + ii * m) + scal(third, nb));
+  };
   if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
   __syncthreads();
   for (int t0 = 0; t0 < n; t0 += NSEG) {
@@ -494,16 +572,16 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
         bool w = seam.wrap(ii, jj, phz);
         out = beta_at(i, w ? phz * x0s[v] : x0s[v]);
       } else {
-        out = beta_at(i, X(i + sd, j));
+        out = beta_inner(i);
       }
-      ring[(t % NRING) * m + v] = out;
+      ring[(t & (NRING - 1)) * m + v] = out;
     }
     __syncthreads();
     for (int t = t0 + ty; t < t1; t += P) {
       cx<R> acc = czero<R>();
       int dmax = t < D ? t : D;
       for (int d = dmax; d >= 0; d--)   // Horner from the farthest term
-        acc = scal(eighth, acc) + ring[((t - d) % NRING) * m + v];
+        acc = scal(eighth, acc) + ring[((t - d) & (NRING - 1)) * m + v];
       Store<S, R>::st(xr + (size_t) (i0 + sd * t) * m, acc);
     }
     __syncthreads();
@@ -520,12 +598,17 @@ __global__ void k_node_prolong(int nc, int m, int K, const double* __restrict__ 
   if (site >= nf * nf) return;
   int i = site % nf, j = site / nf;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  NAcc<S, R> C{c + Lc.node(k, 0, 0, v), nc, m, seam_load<R>(ph, K, k, nc)};
+  const S* cb = c + Lc.node(k, 0, 0, v);
   int ci = i >> 1, cj = j >> 1, oi = i & 1, oj = j & 1;
-  cx<R> val = C(ci, cj);
-  if (oi) val += C(ci + 1, cj);
-  if (oj) val += C(ci, cj + 1);
-  if (oi && oj) val += C(ci + 1, cj + 1);
+  cx<R> val;
+  auto body = [&](const auto& C) {
+    val = C(ci, cj);
+    if (oi) val += C(ci + 1, cj);
+    if (oj) val += C(ci, cj + 1);
+    if (oi && oj) val += C(ci + 1, cj + 1);
+  };
+  if (ci < nc - 1 && cj < nc - 1) body(NAccI<S, R>{cb, nc, m});
+  else body(NAcc<S, R>{cb, nc, m, seam_load<R>(ph, K, k, nc)});
   // weight alpha * (1/2 per odd coordinate): exact powers of two
   if (oi) val = scal(rc<R>(0.5f), val);
   if (oj) val = scal(rc<R>(0.5f), val);
@@ -543,11 +626,15 @@ __global__ void k_node_restrict(int nc, int m, int K, const double* __restrict__
   if (site >= nc * nc) return;
   int i = site % nc, j = site / nc;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
-  NAcc<S, R> F{f + Lf.node(k, 0, 0, v), nf, m, seam_load<R>(ph, K, k, nf)};
+  const S* fb = f + Lf.node(k, 0, 0, v);
   int fi = 2 * i, fj = 2 * j;
-  cx<R> s = F(fi, fj)
-            + scal(rc<R>(0.5f), F(fi - 1, fj) + F(fi + 1, fj) + F(fi, fj - 1) + F(fi, fj + 1))
-            + scal(rc<R>(0.25f), F(fi - 1, fj - 1) + F(fi + 1, fj - 1) + F(fi - 1, fj + 1) + F(fi + 1, fj + 1));
+  cx<R> s;
+  auto body = [&](const auto& F) {
+    s = F(fi, fj) + scal(rc<R>(0.5f), F(fi - 1, fj) + F(fi + 1, fj) + F(fi, fj - 1) + F(fi, fj + 1))
+        + scal(rc<R>(0.25f), F(fi - 1, fj - 1) + F(fi + 1, fj - 1) + F(fi - 1, fj + 1) + F(fi + 1, fj + 1));
+  };
+  if (i > 0 && j > 0) body(NAccI<S, R>{fb, nf, m});
+  else body(NAcc<S, R>{fb, nf, m, seam_load<R>(ph, K, k, nf)});
   S* p = c + Lc.node(k, j, i, v);
   Store<S, R>::st(p, Store<S, R>::ld(p) + scal(sget<R>(alpha), s));
 }
@@ -561,13 +648,20 @@ __global__ void k_gradient(int n, int m, int K, const double* __restrict__ ph, S
   if (site >= n * n) return;
   int i = site % n, j = site / n;
   Lay L{n, m, K};
-  NAcc<SV, R> V{vin + L.node(k, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
-  cx<R> c = V(i, j);
+  const SV* vb = vin + L.node(k, 0, 0, v);
+  cx<R> gx, gy;
+  auto body = [&](const auto& V) {
+    cx<R> c = V(i, j);
+    gx = V(i + 1, j) - c;
+    gy = V(i, j + 1) - c;
+  };
+  if (i < n - 1 && j < n - 1) body(NAccI<SV, R>{vb, n, m});
+  else body(NAcc<SV, R>{vb, n, m, seam_load<R>(ph, K, k, n)});
   R a = sget<R>(alpha);
   SE* px = e + L.edge(k, 0, j, i, v);
   SE* py = e + L.edge(k, 1, j, i, v);
-  Store<SE, R>::st(px, Store<SE, R>::ld(px) + scal(a, V(i + 1, j) - c));
-  Store<SE, R>::st(py, Store<SE, R>::ld(py) + scal(a, V(i, j + 1) - c));
+  Store<SE, R>::st(px, Store<SE, R>::ld(px) + scal(a, gx));
+  Store<SE, R>::st(py, Store<SE, R>::ld(py) + scal(a, gy));
 }
 
 template <typename SE, typename SV, typename R>
@@ -579,9 +673,18 @@ __global__ void k_adjgradient(int n, int m, int K, const double* __restrict__ ph
   if (site >= n * n) return;
   int i = site % n, j = site / n;
   Lay L{n, m, K};
-  EAcc<SE, R> E{e + L.edge(k, 0, 0, 0, v), n, m, seam_load<R>(ph, K, k, n)};
+  const SE* eb = e + L.edge(k, 0, 0, 0, v);
   cx<R> s;
-  if (mass) {
+  if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+    EAccI<SE, R> E{eb, n, m};
+    if (mass) {
+      R mm = sget<R>(sixth);
+      s = mx_x<R>(E, mm, i - 1, j) - mx_x<R>(E, mm, i, j) + mx_y<R>(E, mm, i, j - 1) - mx_y<R>(E, mm, i, j);
+    } else {
+      s = E(0, i - 1, j) - E(0, i, j) + E(1, i, j - 1) - E(1, i, j);
+    }
+  } else if (mass) {
+    EAcc<SE, R> E{eb, n, m, seam_load<R>(ph, K, k, n)};
     // G^H M e: the mass stencil evaluated at the four edges of the node
     R mm = sget<R>(sixth);
     s = mx_x<R>(E, mm, i - 1, j);
@@ -598,6 +701,7 @@ __global__ void k_adjgradient(int n, int m, int K, const double* __restrict__ ph
     }
     s = s - mx_x<R>(E, mm, i, j) + sy - mx_y<R>(E, mm, i, j);
   } else {
+    EAcc<SE, R> E{eb, n, m, seam_load<R>(ph, K, k, n)};
     s = E(0, i - 1, j) - E(0, i, j) + E(1, i, j - 1) - E(1, i, j);
   }
   SV* p = vout + L.node(k, j, i, v);
