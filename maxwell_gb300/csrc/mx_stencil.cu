@@ -1105,6 +1105,8 @@ extern "C" int mxk_adjgradient(int n, int m, int K, const double* ph, double alp
   k_adjgradient<SE, SV, R><<<g, b, 0, st>>>(n, m, K, ph, a, mass, sixth, c, has, (const SE*) e, (SV*) v)
   if (pe == MX_C64 && pv == MX_C64) MX_AG(float2, float2, float);
   else if (pe == MX_C128 && pv == MX_C128) MX_AG(double2, double2, double);
+  // G^H M e of a nearly divergence-free eigenvector is a sum with heavy
+  // cancellation: it is formed in float-float and only then rounded to c64
   else if (pe == MX_CDD && pv == MX_C64) MX_AG(cdd, float2, dd);
   else if (pe == MX_CDD && pv == MX_CDD) MX_AG(cdd, cdd, dd);
   else return (int) cudaErrorInvalidValue;
