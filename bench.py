@@ -253,7 +253,7 @@ def run_ours(args):
         "clocks": clock,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": None,
-                     "kernel": "k_edge_gs_rows (AFW sweep, finest level)", "peak_source": "measured"},
+                     "kernel": "k_edge_gs_colour (AFW sweep in four colours, finest level)", "peak_source": "measured"},
         "fp64_gpu": {"value": fp64_value, "unit": "k-points/s", "k_points": n64,
                      "speedup_mixed_vs_fp64": value / fp64_value, "max_rel_eig_diff_vs_mixed": agree},
         "steps_per_k": float(np.mean([st.mean() for st in steps_all])),

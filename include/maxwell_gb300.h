@@ -108,6 +108,11 @@ int massprod_edge2d_gpu(const edge2d_gpu *x, const edge2d_gpu *y, mxg_field *out
 int gsforward_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
 int gsbackward_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
 int gssymm_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+/* No counterpart in the reference: the same vertex-patch solves in four
+ * vertex colours, (0,0), (1,0), (0,1), (1,1) by (i mod 2, j mod 2), each colour
+ * one parallel pass; dir 0 forward, 1 backward (reverse colour order), 2 both.
+ * The solver's default smoother (mxg_solve_opts.smoother = 1). */
+int gscolour_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x, int dir);
 /* transfers (edge2d.c:5583-5705) */
 int prolongation_edge2d_gpu(mxg_field alpha, const edge2d_gpu *c, edge2d_gpu *f);
 int restriction_edge2d_gpu(mxg_field alpha, const edge2d_gpu *f, edge2d_gpu *c);
@@ -169,6 +174,7 @@ typedef struct {
   int wave;              /* k-points per batch; batch w starts from batch w-1 */
   int relative;          /* stopping rule: 0 absolute defect, 1 relative residual */
   double tol;
+  int smoother;          /* edge smoother: 0 the reference's row order, 1 four colours */
 } mxg_solve_opts;
 
 typedef struct mxg_solver mxg_solver;

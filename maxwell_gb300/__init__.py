@@ -35,7 +35,8 @@ def fz(z) -> Field:
 class SolveOpts(C.Structure):
     _fields_ = [(n, C.c_int) for n in (
         "n0", "L", "ieigs", "m", "method", "precision", "max_nested", "max_steps", "prec_steps",
-        "gradient_steps", "smoother_steps", "lift_e", "center", "wave", "relative")] + [("tol", C.c_double)]
+        "gradient_steps", "smoother_steps", "lift_e", "center", "wave", "relative")] + [("tol", C.c_double),
+                                                                                  ("smoother", C.c_int)]
 
 
 def lib() -> C.CDLL:
@@ -69,6 +70,7 @@ def lib() -> C.CDLL:
             "gsforward_edge2d_gpu": (I, [Field, Field, P, P]),
             "gsbackward_edge2d_gpu": (I, [Field, Field, P, P]),
             "gssymm_edge2d_gpu": (I, [Field, Field, P, P]),
+            "gscolour_edge2d_gpu": (I, [Field, Field, P, P, I]),
             "prolongation_edge2d_gpu": (I, [Field, P, P]),
             "restriction_edge2d_gpu": (I, [Field, P, P]),
             "vcycle_edge2d_gpu": (I, [I, I, P, P, P, P]),
@@ -262,9 +264,9 @@ class Solver:
 
     def __init__(self, kappa_fine, *, n0, L, ieigs, m, method=1, precision=1, max_nested=20,
                  max_steps=60, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1, center=1,
-                 wave=1, relative=1, tol=1e-8):
+                 wave=1, relative=1, tol=1e-8, smoother=1):
         self.o = SolveOpts(n0, L, ieigs, m, method, precision, max_nested, max_steps, prec_steps,
-                           gradient_steps, smoother_steps, lift_e, center, wave, relative, tol)
+                           gradient_steps, smoother_steps, lift_e, center, wave, relative, tol, smoother)
         self.n = n0 << L
         self.m, self.wave = m, wave
         k = np.ascontiguousarray(kappa_fine, np.float64)

@@ -401,6 +401,14 @@ int gsforward_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_
 int gsbackward_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x) { return gs_e(creal_(a), creal_(b), bb, x, 1); }
 int gssymm_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x) { return gs_e(creal_(a), creal_(b), bb, x, 2); }
 
+int gscolour_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x, int dir)
+{
+  const grid2d_gpu *g = x->gr;
+  if(!same_shape_e(bb, x) || bb->prec != x->prec || dir < 0 || dir > 2) return MXG_EINVAL;
+  return mxk_edge_gs_colour(g->n, x->m, g->K, g->ph, kap_of(g), creal_(a), creal_(b), dir, x->prec, bb->d, x->d,
+                            g->st);
+}
+
 int prolongation_edge2d_gpu(mxg_field alpha, const edge2d_gpu *c, edge2d_gpu *f)
 {
   if(f->gr->n != 2 * c->gr->n || c->m != f->m || c->prec != f->prec || c->gr->K != f->gr->K) return MXG_EINVAL;

@@ -51,6 +51,11 @@ int mxk_edge_apply(int n, int m, int K, const double *phases, mxk_kappa kap,
 int mxk_edge_gs(int n, int m, int K, const double *phases, mxk_kappa kap,
                 double alpha, double beta, int dir, int prec,
                 const void *b, void *x, mx_stream s);
+/* the same smoother in four vertex colours (each colour one parallel launch):
+ * forward (0,0), (1,0), (0,1), (1,1), backward the reverse order */
+int mxk_edge_gs_colour(int n, int m, int K, const double *phases, mxk_kappa kap,
+                       double alpha, double beta, int dir, int prec,
+                       const void *b, void *x, mx_stream s);
 int mxk_edge_prolong(int nc, int m, int K, const double *phases, double alpha,
                      int prec, const void *c, void *f, mx_stream s);
 int mxk_edge_restrict(int nc, int m, int K, const double *phases, double alpha,

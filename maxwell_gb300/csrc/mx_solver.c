@@ -141,7 +141,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   size_t es_g, es_e;
   double *kk[MAXL];
   if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 16
-     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1)
+     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 1)
     return 0;
   s = calloc(1, sizeof(mxg_solver));
   s->o = *o;
@@ -307,8 +307,14 @@ static int edge_gs(mxg_solver *s, int l, int dir)
     if(s->npev + 2 > s->maxpev) prof_flush(s);
     cudaEventRecord(s->pev[s->npev++], s->st);
   }
-  e = mxk_edge_gs(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
-  s->launches += 2 * (dir == 2 ? 2 : 1);
+  if(s->o.smoother) {
+    e = mxk_edge_gs_colour(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
+    s->launches += 4 * (dir == 2 ? 2 : 1);
+  }
+  else {
+    e = mxk_edge_gs(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
+    s->launches += 2 * (dir == 2 ? 2 : 1);
+  }
   if(timed) cudaEventRecord(s->pev[s->npev++], s->st);
   return e;
 }

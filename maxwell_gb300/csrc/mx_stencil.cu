@@ -399,6 +399,104 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
 }
 
 // ------------------------------------------------------------------
+// AFW vertex-patch smoother in four colours.  The vertices (i, j) split by
+// (i mod 2, j mod 2); two patches of one colour share no unknown, and none
+// reads an unknown the other writes (a patch writes x(i-1..i, j) and
+// y(i, j-1..j) and reads x(i-1..i, j-1..j+1), y(i-1..i+1, j-1..j)), so one
+// launch solves every patch of a colour at once: one thread per (patch,
+// vector, k-point), the same local solve as the row sweep.  A forward sweep
+// takes the colours (0,0), (1,0), (0,1), (1,1), a backward sweep the reverse
+// order.  The iterates differ from the reference's row order; both are
+// convergent splittings of the same operator, so the eigenpairs the solver
+// converges to are the same.
+// ------------------------------------------------------------------
+template <typename S, typename R>
+__device__ __forceinline__ void st_edge(S* base, int n, int m, const Seam<R>& seam, int p, int i, int j, cx<R> v) {
+  cx<R> ph;
+  if (seam.wrap(i, j, ph)) v = conjc(ph) * v;
+  Store<S, R>::st(base + ((p * n + j) * n + i) * m, v);
+}
+
+template <typename S, typename R>
+__global__ void k_edge_gs_colour(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
+                                 const float4* __restrict__ ftab, Sc axy_s, Sc mm_s, Sc s8_s, Sc is8_s, int ci,
+                                 int cj, const S* __restrict__ b, S* x) {
+  // block (m, rows): x = vector, y = patch of the colour; grid.y = k-point
+  const int h = n / 2;
+  const int k = blockIdx.y, v = threadIdx.x;
+  const int q = blockIdx.x * blockDim.y + threadIdx.y;
+  if (q >= h * h) return;
+  const int i = 2 * (q % h) + ci, j = 2 * (q / h) + cj;
+  Lay L{n, m, K};
+  S* xb = x + L.edge(k, 0, 0, 0, v);
+  const S* bb = b + L.edge(k, 0, 0, 0, v);
+  const R axy = sget<R>(axy_s), mm = sget<R>(mm_s), s8 = sget<R>(s8_s), is8 = sget<R>(is8_s);
+  const R four = rc<R>(4.0f), quarter = rc<R>(0.25f);
+  const bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
+  cx<R> xa0, xa1, xa2, xb0, xb1, xb2, ya0, ya1, yb0, yb1, yc0, yc1, bx0, bx1, by0, by1;
+  R kLL, kUL, kLR, kUR;
+  auto gather = [&](const auto& X, const auto& B, const auto& KA) {
+    xa0 = X(0, i - 1, j - 1); xa1 = X(0, i - 1, j); xa2 = X(0, i - 1, j + 1);
+    xb0 = X(0, i, j - 1); xb1 = X(0, i, j); xb2 = X(0, i, j + 1);
+    ya0 = X(1, i - 1, j - 1); ya1 = X(1, i - 1, j);
+    yb0 = X(1, i, j - 1); yb1 = X(1, i, j);
+    yc0 = X(1, i + 1, j - 1); yc1 = X(1, i + 1, j);
+    bx0 = B(0, i - 1, j); bx1 = B(0, i, j); by0 = B(1, i, j - 1); by1 = B(1, i, j);
+    kLL = KA(i - 1, j - 1); kUL = KA(i - 1, j); kLR = KA(i, j - 1); kUR = KA(i, j);
+  };
+  Seam<R> seam;
+  if (inner) {
+    gather(EAccI<S, R>{xb, n, m}, EAccI<S, R>{bb, n, m}, KapI<R>{kap});
+  } else {
+    seam = seam_load<R>(ph, K, k, n);
+    gather(EAcc<S, R>{xb, n, m, seam}, EAcc<S, R>{bb, n, m, seam}, kap);
+  }
+  cx<R> cLL = xa0 - xa1 - ya0 + yb0;
+  cx<R> cUL = xa1 - xa2 - ya1 + yb1;
+  cx<R> cLR = xb0 - xb1 - yb0 + yc0;
+  cx<R> cUR = xb1 - xb2 - yb1 + yc1;
+  cx<R> r0 = bx0 - (scal(axy, scal(kUL, cUL) - scal(kLL, cLL)) + scal(mm, scal(four, xa1) + xa2 + xa0));
+  cx<R> r1 = bx1 - (scal(axy, scal(kUR, cUR) - scal(kLR, cLR)) + scal(mm, scal(four, xb1) + xb2 + xb0));
+  cx<R> r2 = by0 - (scal(axy, scal(kLL, cLL) - scal(kLR, cLR)) + scal(mm, scal(four, yb0) + yc0 + ya0));
+  cx<R> r3 = by1 - (scal(axy, scal(kUL, cUL) - scal(kUR, cUR)) + scal(mm, scal(four, yb1) + yc1 + ya1));
+  R l20, l21, i0, i1, i2;
+  if (ftab) {
+    float4 fa = ftab[2 * (j * n + i)];
+    l20 = Real<R>::from_float(fa.x); l21 = Real<R>::from_float(fa.y);
+    i0 = Real<R>::from_float(fa.z); i1 = Real<R>::from_float(fa.w);
+    i2 = Real<R>::from_float(ftab[2 * (j * n + i) + 1].x);
+  } else {
+    afw_factors<R>(kLL, kUL, kLR, kUR, axy, s8, l20, l21, i0, i1, i2);
+  }
+  cx<R> c0 = r0 + r1 + r2 + r3;
+  cx<R> c1 = r0 + r1 - r2 - r3;
+  cx<R> c2 = r0 - r1 - r2 + r3;
+  cx<R> c3 = r0 - r1 + r2 - r3;
+  c2 -= scal(l20, c0) + scal(l21, c1);
+  c0 = scal(i0, c0);
+  c1 = scal(i1, c1);
+  c2 = scal(i2, c2);
+  c3 = scal(is8, c3);
+  c1 -= scal(l21, c2);
+  c0 -= scal(l20, c2);
+  xa1 += scal(quarter, c0 + c1 + c2 + c3);
+  xb1 += scal(quarter, c0 + c1 - c2 - c3);
+  yb0 += scal(quarter, c0 - c1 - c2 + c3);
+  yb1 += scal(quarter, c0 - c1 + c2 - c3);
+  if (inner) {
+    Store<S, R>::st(xb + (j * n + i - 1) * m, xa1);
+    Store<S, R>::st(xb + (j * n + i) * m, xb1);
+    Store<S, R>::st(xb + ((n + j - 1) * n + i) * m, yb0);
+    Store<S, R>::st(xb + ((n + j) * n + i) * m, yb1);
+  } else {
+    st_edge<S, R>(xb, n, m, seam, 0, i - 1, j, xa1);
+    st_edge<S, R>(xb, n, m, seam, 0, i, j, xb1);
+    st_edge<S, R>(xb, n, m, seam, 1, i, j - 1, yb0);
+    st_edge<S, R>(xb, n, m, seam, 1, i, j, yb1);
+  }
+}
+
+// ------------------------------------------------------------------
 // edge transfers (gather form of prolongation_edge2d / restriction_edge2d)
 // ------------------------------------------------------------------
 template <typename S, typename R>
@@ -881,6 +979,18 @@ extern "C" size_t mxk_elem_size(int prec) { return prec == MX_C64 ? 8 : 16; }
    : (int) cudaErrorInvalidValue)
 
 template <typename S, typename R>
+static int L_edge_gs_colour(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha, double beta,
+                            int ci, int cj, const void* b, void* x, cudaStream_t st) {
+  const float4* ftab = (sizeof(R) == 4 && kap.afw && kap.afw_alpha == alpha && kap.afw_beta == beta)
+                           ? (const float4*) kap.afw : nullptr;
+  size_t patches = (size_t) (n / 2) * (n / 2);
+  k_edge_gs_colour<S, R><<<grd2(patches, m, K), blk2(m), 0, st>>>(
+      n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
+      make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), ci, cj, (const S*) b, (S*) x);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+template <typename S, typename R>
 static int L_edge_gs_rows(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
                           double beta, int j0, int jstep, int nrows, int backward, const void* b,
                           void* x, cudaStream_t st) {
@@ -1030,6 +1140,25 @@ extern "C" int mxk_edge_gs(int n, int m, int K, const double* ph, mxk_kappa kap,
     if ((e = MX_BY_PREC(prec, L_edge_gs_rows, n, m, K, ph, kap, alpha, beta, 1, 2, half, 1, b, x, st))) return e;
     if ((e = MX_BY_PREC(prec, L_edge_gs_rows, n, m, K, ph, kap, alpha, beta, 0, 2, half, 1, b, x, st))) return e;
   }
+  return 0;
+}
+
+extern "C" int mxk_edge_gs_colour(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
+                                  double beta, int dir, int prec, const void* b, void* x, mx_stream s) {
+  static const int order[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
+  cudaStream_t st = (cudaStream_t) s;
+  int e;
+  if (n < 2 || (n & 1) || m < 1 || m > 256) return (int) cudaErrorInvalidValue;
+  if (dir == 0 || dir == 2)
+    for (int c = 0; c < 4; c++)
+      if ((e = MX_BY_PREC(prec, L_edge_gs_colour, n, m, K, ph, kap, alpha, beta, order[c][0], order[c][1], b, x,
+                          st)))
+        return e;
+  if (dir == 1 || dir == 2)
+    for (int c = 3; c >= 0; c--)
+      if ((e = MX_BY_PREC(prec, L_edge_gs_colour, n, m, K, ph, kap, alpha, beta, order[c][0], order[c][1], b, x,
+                          st)))
+        return e;
   return 0;
 }
 

@@ -322,6 +322,40 @@ om_gs_edge(int n, const double *kappa, cx xf, cx yf, cx alpha, cx beta,
     gs_edge_dir(n, kappa, xf, yf, alpha, beta, 1, b, x);
 }
 
+/* The four-colour order of the same patch solves (the GPU solver's
+ * smoother; it has no counterpart in the reference): vertices split by
+ * (i mod 2, j mod 2), forward (0,0), (1,0), (0,1), (1,1), backward the
+ * reverse.  Patches of one colour do not read each other's unknowns, so the
+ * order inside a colour does not matter. */
+static void
+gs_edge_colour(int n, const double *kappa, cx xf, cx yf, double axy, double mm, cx ax_, cx mx_,
+               const cx *b, cx *x, int ci, int cj)
+{
+  int j;
+#pragma omp parallel for schedule(static)
+  for(j = cj; j < n; j += 2) {
+    int i;
+    for(i = ci; i < n; i += 2)
+      patch_solve(n, kappa, xf, yf, axy, mm, ax_, mx_, b, x, i, j);
+  }
+}
+
+void
+om_gs_edge_colour(int n, const double *kappa, cx xf, cx yf, cx alpha, cx beta,
+                  int dir, const cx *b, cx *x)
+{
+  static const int order[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
+  double axy = creal(alpha) * n * (double) n, mm = creal(beta) / 6.0;
+  cx ax_ = alpha * (double) n * (double) n, mx_ = beta / 6.0;
+  int c;
+  if(dir == 0 || dir == 2)
+    for(c = 0; c < 4; c++)
+      gs_edge_colour(n, kappa, xf, yf, axy, mm, ax_, mx_, b, x, order[c][0], order[c][1]);
+  if(dir == 1 || dir == 2)
+    for(c = 3; c >= 0; c--)
+      gs_edge_colour(n, kappa, xf, yf, axy, mm, ax_, mx_, b, x, order[c][0], order[c][1]);
+}
+
 /* ------------------------------------------------------------
  * Edge transfers   (edge2d.c:5583-5705)
  * ------------------------------------------------------------ */

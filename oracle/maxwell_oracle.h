@@ -32,6 +32,9 @@ double om_norm2(long len, const om_cplx *x);
 void om_gs_edge(int n, const double *kappa, om_cplx xf, om_cplx yf,
                 om_cplx alpha, om_cplx beta, int dir,
                 const om_cplx *b, om_cplx *x);
+/* the same patch solves in four vertex colours (the GPU solver's order) */
+void om_gs_edge_colour(int n, const double *kappa, om_cplx xf, om_cplx yf,
+                       om_cplx alpha, om_cplx beta, int dir, const om_cplx *b, om_cplx *x);
 void om_prolong_edge(int nc, om_cplx xf, om_cplx yf, om_cplx alpha,
                      const om_cplx *c, om_cplx *f);
 void om_restrict_edge(int nc, om_cplx xf, om_cplx yf, om_cplx alpha,

@@ -93,6 +93,12 @@ class Oracle:
                             _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
         return x
 
+    def gs_edge_colour(self, n, kappa, xf, yf, alpha, beta, direction, b, x):
+        x = _cvec(x).copy()
+        self.lib.om_gs_edge_colour(C.c_int(n), _p(np.ascontiguousarray(kappa, np.float64)), _cz(xf), _cz(yf),
+                                   _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
+        return x
+
     def prolong_edge(self, nc, xf, yf, alpha, c, f):
         f = _cvec(f).copy()
         self.lib.om_prolong_edge(C.c_int(nc), _cz(xf), _cz(yf), _cz(alpha), _p(_cvec(c)), _p(f))

@@ -46,7 +46,8 @@ def test_solver_rejects_bad_options(built):
     bad = [mx.SolveOpts(7, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8),    # odd n0
            mx.SolveOpts(8, 1, 8, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8),    # ieigs > m
            mx.SolveOpts(8, 1, 4, 40, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8),   # m > 16
-           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 0, 1, 1e-8)]    # wave 0
+           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 0, 1, 1e-8),    # wave 0
+           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8, 2)]  # no such smoother
     for o in bad:
         assert not mx.lib().mxg_solver_new(C.byref(o), np.ones(256).ctypes.data_as(C.c_void_p))
 

@@ -79,6 +79,37 @@ def test_afw_smoother(oracle, setup, prec, direction):
     assert rel(ex.get(), want) < (1e-11 if prec == mx.C128 else 1e-4)
 
 
+@pytest.mark.parametrize("prec", [mx.C128, mx.CDD, mx.C64])
+@pytest.mark.parametrize("direction", [0, 1, 2])
+def test_colour_smoother(oracle, setup, prec, direction):
+    """The four-colour patch smoother (gscolour_edge2d_gpu) against the
+    oracle's restatement of the same order."""
+    rng, n, K, m, kap = setup
+    g = mx.Grid(n, K, kap, FACTORS)
+    b, x = cv(rng, K, m, 2 * n * n), cv(rng, K, m, 2 * n * n)
+    eb, ex = mx.Edge(g, m, prec, b), mx.Edge(g, m, prec, x)
+    mx.check(mx.lib().gscolour_edge2d_gpu(mx.fz(1.0), mx.fz(1.0), eb.h, ex.h, direction))
+    want = np.array([[oracle.gs_edge_colour(n, kap, *FACTORS[k], 1.0, 1.0, direction, b[k, v], x[k, v])
+                      for v in range(m)] for k in range(K)])
+    assert rel(ex.get(), want) < (1e-11 if prec != mx.C64 else 1e-4)
+
+
+@pytest.mark.parametrize("smoother", [0, 1])
+def test_solver_smoothers_agree(oracle, smoother):
+    """Both edge smoothers drive the mixed LOBPCG to the same eigenvalues."""
+    n0, L = 8, 2
+    n = n0 << L
+    kap = oracle.disc_kappa(n, [[12.0, 0.5, 0.5, 0.3]], 1.0)
+    fac = np.array([[np.exp(0.4j), np.exp(1.1j)], [np.exp(2.5j), 1.0]])
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=8, m=12, method=1, precision=1, wave=2, relative=1, tol=1e-9,
+                  max_nested=5, max_steps=60, smoother=smoother)
+    lam, steps, res = s.solve(fac)
+    st, lam_o, _, _, _ = oracle.bloch_solve(kap, fac, n0=n0, L=L, ieigs=8, m=12, method=1, max_nested=40,
+                                            max_steps=60, tol=1e-9, relative=1, extrapolation="n", wave=2)
+    assert res[:, :8].max() <= 1e-9
+    assert np.abs(lam[:, :8] - lam_o[:, :8]).max() / lam_o[:, :8].max() < 1e-8
+
+
 @pytest.mark.parametrize("prec", [mx.C128, mx.C64])
 def test_transfers_node_ops_gradient(oracle, setup, prec):
     rng, n, K, m, kap = setup

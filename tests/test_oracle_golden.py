@@ -174,3 +174,25 @@ def test_oracle_adjoint_matches_finite_differences(oracle):
         em[c] -= h
         fd = (solve(ep)[0][0, band] - solve(em)[0][0, band]) / (2 * h)
         assert abs(fd - g[c]) <= 1e-5 * np.abs(g).max(), (c, fd, g[c])
+
+
+def test_oracle_colour_smoother_converges(oracle, golden):
+    """The four-colour patch smoother (the GPU solver's order) is a convergent
+    splitting of alpha A + beta M: symmetric sweeps shrink the error of
+    (A + M) x = b in the energy norm, every sweep."""
+    g = golden("ops_n16.npz")
+    n, kap, xf, yf = int(g["n"]), g["kappa_gen"], complex(g["xf"]), complex(g["yf"])
+    rng = np.random.default_rng(4)
+    xs = rng.standard_normal(2 * n * n) + 1j * rng.standard_normal(2 * n * n)
+    b = oracle.addeval_edge(n, kap, xf, yf, 1.0, 1.0, xs, np.zeros_like(xs))
+    x = np.zeros_like(xs)
+
+    def energy(e):
+        return np.real(np.vdot(e, oracle.addeval_edge(n, kap, xf, yf, 1.0, 1.0, e, np.zeros_like(e))))
+
+    last = energy(x - xs)
+    for _ in range(6):
+        x = oracle.gs_edge_colour(n, kap, xf, yf, 1.0, 1.0, 2, b, x)
+        cur = energy(x - xs)
+        assert cur < 0.9 * last
+        last = cur
