@@ -572,6 +572,7 @@ static int cold_start(mxg_solver *s, int K_active)
   double *th = malloc(sizeof(double) * N * K), *cf = malloc(sizeof(double) * 2 * (size_t) N * N * K);
   double *e0 = malloc(sizeof(double) * 2 * (size_t) K * N * m);
   int e = 0;
+  double t0 = now_s();
   L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 1.0, 0.0, s->cA, s->st));
   L_(mxk_dense_edge(s->n0, K, s->ph, kap(s, 0), 0.0, 1.0, s->cM, s->st));
   L_(mxk_rayleigh_ritz(N, N, K, s->cA, s->cM, 0, 1e-14, -1e300, s->ccoef, s->ctheta, s->cinfo, s->cwork, s->st));
@@ -579,6 +580,7 @@ static int cold_start(mxg_solver *s, int K_active)
   if(!e) e = (int) cudaMemcpyAsync(cf, s->ccoef, sizeof(double) * 2 * (size_t) N * N * K, cudaMemcpyDeviceToHost, s->st);
   if(!e) e = (int) cudaStreamSynchronize(s->st);
   if(e) { free(th); free(cf); free(e0); return e; }
+  if(s->timing) fprintf(stderr, "  coarse eigenproblem %.3f s\n", now_s() - t0);
   /* skip |lambda| < 1e-8 (exp_bloch2d.c:546-551); level-0 block layout of
    * one k is row-major N x m */
   for(k = 0; k < K; k++) {
@@ -622,7 +624,12 @@ static int cold_start(mxg_solver *s, int K_active)
     TRY(residual(s, l, 0));
     for(k = 0; k < K * m; k++) s->h_mu[k] = s->h_rq[k];
     TRY(upload_mu(s));
+    t0 = now_s();
     TRY(iterate(s, l, l == s->L ? s->o.max_steps : s->o.max_nested, K_active));
+    if(s->timing) {
+      cudaStreamSynchronize(s->st);
+      fprintf(stderr, "  level %d (n = %d): %.3f s\n", l, s->n[l], now_s() - t0);
+    }
   }
   return 0;
 }
