@@ -619,10 +619,13 @@ constexpr int NSEG = 64, NRING = 128;   // ring: a power of two >= NSEG + D
 template <typename S, typename R, int D>
 __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s,
                               int j0, int jstep, int backward, const S* __restrict__ b, S* x) {
-  static_assert(NRING >= NSEG + D, "ring too short for the prefix depth");
+  // FP32 rows take longer segments (fewer barrier rounds per row); the
+  // float-float and FP64 rings, twice as wide per entry, keep the shorter ones
+  constexpr int SEG = D == 8 ? 2 * NSEG : NSEG, RING = D == 8 ? 2 * NRING : NRING;
+  static_assert(RING >= SEG + D && (RING & (RING - 1)) == 0, "ring too short for the prefix depth");
   extern __shared__ float smn[];
-  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);   // NRING * m
-  cx<R>* x0s = ring + NRING * m;                  // m
+  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);   // RING * m
+  cx<R>* x0s = ring + RING * m;                  // m
   int k = blockIdx.y, v = threadIdx.x, P = blockDim.y, ty = threadIdx.y;
   int j = j0 + blockIdx.x * jstep;
   Lay L{n, m, K};
@@ -657,8 +660,8 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
   };
   if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
   __syncthreads();
-  for (int t0 = 0; t0 < n; t0 += NSEG) {
-    int t1 = t0 + NSEG < n ? t0 + NSEG : n;
+  for (int t0 = 0; t0 < n; t0 += SEG) {
+    int t1 = t0 + SEG < n ? t0 + SEG : n;
     for (int t = t0 + ty; t < t1; t += P) {
       int i = i0 + sd * t;
       cx<R> out;
@@ -672,14 +675,14 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
       } else {
         out = beta_inner(i);
       }
-      ring[(t & (NRING - 1)) * m + v] = out;
+      ring[(t & (RING - 1)) * m + v] = out;
     }
     __syncthreads();
     for (int t = t0 + ty; t < t1; t += P) {
       cx<R> acc = czero<R>();
       int dmax = t < D ? t : D;
       for (int d = dmax; d >= 0; d--)   // Horner from the farthest term
-        acc = scal(eighth, acc) + ring[((t - d) & (NRING - 1)) * m + v];
+        acc = scal(eighth, acc) + ring[((t - d) & (RING - 1)) * m + v];
       Store<S, R>::st(xr + (size_t) (i0 + sd * t) * m, acc);
     }
     __syncthreads();
@@ -1033,7 +1036,7 @@ template <typename S, typename R>
 static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, int j0, int jstep,
                           int nrows, int backward, const void* b, void* x, cudaStream_t st) {
   dim3 g(nrows, K), b2 = blk2(m);
-  size_t smem = (size_t) (NRING + 1) * m * sizeof(cx<R>);
+  size_t smem = (size_t) ((sizeof(R) == 4 ? 2 * NRING : NRING) + 1) * m * sizeof(cx<R>);
   Sc inv_ac = make_sc(3.0 / (8.0 * alpha)), third = make_sc(alpha / 3.0);
   // 8^-(D+1) below the unit roundoff: D = 8 for FP32, 18 for FP64 and float-float
   if (sizeof(R) == 4) {
