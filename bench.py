@@ -77,6 +77,26 @@ def dist_env():
     return ws, rank
 
 
+def rank_kpoints(ws: int, rank: int) -> np.ndarray:
+    """The k-points of one rank: every ws-th point of a 32*ws-point path, so
+    each rank solves NK independent k-points (weak scaling) and the ranks
+    together cover the path once."""
+    return gamma_x_m_gamma(NK * ws)[rank::ws]
+
+
+def max_over_ranks(values):
+    """Element-wise maximum of per-rank timings (no-op on one process)."""
+    if int(os.environ.get("WORLD_SIZE", "1")) == 1:
+        return [float(v) for v in values]
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -173,7 +193,7 @@ def run_ours(args):
         raise RuntimeError("no CUDA device")
     n = N0 << LEVELS
     kap = disc_kappa(n)
-    kpts = gamma_x_m_gamma(NK * ws)[rank::ws]
+    kpts = rank_kpoints(ws, rank)
     fac = factors_of(kpts)
 
     def make(precision, wave):
@@ -202,11 +222,7 @@ def run_ours(args):
     kms, kcount, kbytes = s.kernel_time()
     s.profile(False)
     t_dev = dev_ms / 1e3
-    if ws > 1:
-        import torch
-        tt = torch.tensor([t_dev, wall], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, wall = float(tt[0]), float(tt[1])
+    t_dev, wall = max_over_ranks([t_dev, wall])
     value = NK * ws * args.steps / t_dev
 
     # e2e: through the public API from host buffers -- solver creation
