@@ -203,7 +203,6 @@ def run_ours(args):
     s = make(1, NK)
     for _ in range(args.warmup):
         s.solve(fac)
-    s.profile(True)
     clocks = Clocks()
     clocks.start()
     if ws > 1:
@@ -219,11 +218,17 @@ def run_ours(args):
         res_max = max(res_max, float(res[:, :IEIGS].max()))
     wall = time.time() - t0
     clock = clocks.stop()
-    kms, kcount, kbytes = s.kernel_time()
-    s.profile(False)
     t_dev = dev_ms / 1e3
     t_dev, wall = max_over_ranks([t_dev, wall])
     value = NK * ws * args.steps / t_dev
+
+    # the roofline kernel: one more solve with its finest-level AFW sweeps
+    # bracketed by CUDA events on the solver's stream (the timed solves above
+    # replay CUDA graphs, whose inner launches carry no events)
+    s.profile(True)
+    s.solve(fac)
+    kms, kcount, kbytes = s.kernel_time()
+    s.profile(False)
 
     # e2e: through the public API from host buffers -- solver creation
     # uploads kappa (h2d), the solve takes the k-points from host memory and

@@ -83,6 +83,11 @@ struct mxg_solver {
   double prof_ms;
   long prof_count;
   int prof_step, prof_done;          /* profiler window (MXG_PROFILE_STEP) */
+  /* CUDA graphs of the inner multigrid loops, one per level: the edge
+   * V-cycles of the preconditioner and the node V-cycles of a lifting */
+  cudaGraphExec_t gpre[MAXL], glift[MAXL];
+  long gpre_n[MAXL], glift_n[MAXL];   /* kernel launches each graph holds */
+  int graphs;                          /* 1 capture and replay, 0 launch directly */
 };
 
 #define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
@@ -109,6 +114,8 @@ void mxg_solver_free(mxg_solver *s)
   int l;
   if(!s) return;
   for(l = 0; l <= s->L; l++) {
+    if(s->gpre[l]) cudaGraphExecDestroy(s->gpre[l]);
+    if(s->glift[l]) cudaGraphExecDestroy(s->glift[l]);
     cudaFree(s->kd[l]); cudaFree(s->kf[l]); cudaFree(s->kdd[l]); cudaFree(s->kafw[l]);
     cudaFree(s->b[l]); cudaFree(s->x[l]); cudaFree(s->d[l]);
     cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
@@ -231,6 +238,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   s->h_conv = malloc(sizeof(int) * K);
   s->h_steps = malloc(sizeof(int) * K);
   s->timing = getenv("MXG_TIMING") != 0;
+  s->graphs = getenv("MXG_NO_GRAPHS") == 0;
   /* MXG_PROFILE_STEP=q brackets finest-level block step q of the first wave
    * with cudaProfilerStart/Stop, for a profiler started with profiling off */
   s->prof_step = getenv("MXG_PROFILE_STEP") ? atoi(getenv("MXG_PROFILE_STEP")) : -1;
@@ -370,26 +378,74 @@ static int vcycle_n(mxg_solver *s, int top)
 }
 
 /* gradient lifting (exp_bloch2d.c:971-978): y -= G L^-1 G^H M y */
-static int lift(mxg_solver *s, int l, int py, void *y)
+/* Runs body(s, l) on the solver's stream through a CUDA graph of level l:
+ * captured at the first call, replayed afterwards (every pointer the bodies
+ * use is fixed for the solver's lifetime).  With profiling on, or if the
+ * capture fails, the body launches directly. */
+static int run_graphed(mxg_solver *s, int l, cudaGraphExec_t *exec, long *nlaunch,
+                       int (*body)(mxg_solver *, int))
 {
-  int i, n = s->n[l];
-  if(s->o.gradient_steps <= 0) return 0;
-  L_(mxk_adjgradient(n, s->m, s->K, s->ph, 1.0, 1, 0.0, py, y, s->pg, s->bg[l], s->st));
+  cudaGraph_t g = 0;
+  long before;
+  int e;
+  if(!s->graphs || s->prof) return body(s, l);
+  if(!*exec) {
+    if(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      s->graphs = 0;
+      return body(s, l);
+    }
+    before = s->launches;
+    e = body(s, l);
+    if(cudaStreamEndCapture(s->st, &g) != cudaSuccess || e || !g
+       || cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+      if(g) cudaGraphDestroy(g);
+      *exec = 0;
+      cudaGetLastError();
+      s->graphs = 0;
+      s->launches = before;
+      return body(s, l);
+    }
+    cudaGraphDestroy(g);
+    *nlaunch = s->launches - before;
+    s->launches = before;
+  }
+  s->launches += *nlaunch;
+  return (int) cudaGraphLaunch(*exec, s->st);
+}
+
+static int lift_body(mxg_solver *s, int l)
+{
+  int i;
   L_(mxk_zero(s->pg, s->xg[l], nlen(s, l), s->st));
   for(i = 0; i < s->o.gradient_steps; i++)
     TRY(vcycle_n(s, l));
+  return 0;
+}
+
+static int lift(mxg_solver *s, int l, int py, void *y)
+{
+  int n = s->n[l];
+  if(s->o.gradient_steps <= 0) return 0;
+  L_(mxk_adjgradient(n, s->m, s->K, s->ph, 1.0, 1, 0.0, py, y, s->pg, s->bg[l], s->st));
+  TRY(run_graphed(s, l, &s->glift[l], &s->glift_n[l], lift_body));
   L_(mxk_gradient(n, s->m, s->K, s->ph, -1.0, s->pg, s->xg[l], py, y, s->st));
   return 0;
 }
 
-/* x[l] = V^prec b[l] from zero */
-static int precondition(mxg_solver *s, int l)
+static int precondition_body(mxg_solver *s, int l)
 {
   int i;
   L_(mxk_zero(s->pg, s->x[l], elen(s, l), s->st));
   for(i = 0; i < s->o.prec_steps; i++)
     TRY(vcycle_e(s, l));
   return 0;
+}
+
+/* x[l] = V^prec b[l] from zero */
+static int precondition(mxg_solver *s, int l)
+{
+  return run_graphed(s, l, &s->gpre[l], &s->gpre_n[l], precondition_body);
 }
 
 /* residual of E (rhs for the preconditioner into b[l]) and its statistics;
