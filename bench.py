@@ -341,6 +341,41 @@ def run_kernels(args):
                           "frac": gbs / hbm}), flush=True)
 
 
+def run_surface(args):
+    """The full-zone surface (exp_blochsurf): 256^2 cells, four discs eps = 10
+    of radius 0.15 centred at (0.25|0.75, 0.25|0.75), a 32 x 32 k-grid over
+    [-pi, pi]^2 solved in waves of 64 (each wave starting from the previous
+    one), 12 pairs with block 16 via LOBPCG, mixed precision, relative
+    residual 1e-8.  Not the headline metric: one JSON line of k-points/s."""
+    import maxwell_gb300 as mx
+    n0, L, steps, wave = 8, 5, 32, 64
+    n = n0 << L
+    h = 1.0 / n
+    i = np.arange(n)
+    X, Y = np.meshgrid(i * h, i * h)
+    inside = np.zeros_like(X, dtype=bool)
+    for cy in (0.25, 0.75):
+        for cx in (0.25, 0.75):
+            inside |= (X - cx) ** 2 + (Y - cy) ** 2 <= 0.15 ** 2
+    kap = np.ascontiguousarray(np.where(inside, 1.0 / 10.0, 1.0).reshape(-1))
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=IEIGS, m=BLOCK, method=1, precision=1, max_nested=MAX_NESTED,
+                  max_steps=60, wave=wave, relative=1, tol=TOL)
+    for _ in range(args.warmup):
+        s.solve(factors_of(gamma_x_m_gamma(wave)))
+    t0 = time.time()
+    lam, st, res = s.surface(steps)
+    wall = time.time() - t0
+    ms, nl = s.stats()
+    print(json.dumps({"metric": "k-points/s, full-zone surface 256^2, 32x32 k-grid in waves of 64",
+                      "value": steps * steps / (ms / 1e3), "unit": "k-points/s", "wall_s": wall,
+                      "steps_first_wave": float(st.reshape(-1)[:wave].mean()),
+                      "steps_later_waves": float(st.reshape(-1)[wave:].mean()),
+                      "max_rel_residual": float(res[..., :IEIGS].max()), "gpu_launches": nl,
+                      "config": {"workload": "256^2, 4 discs eps=10 r=0.15, 32x32 k-grid over the zone, "
+                                             "waves of 64, 12 pairs block 16, LOBPCG, relative residual 1e-8"}}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,9 +386,12 @@ def main():
     ap.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead of the metric")
     ap.add_argument("--nk", type=int, default=NK, help="k-points of the --kernels table")
     ap.add_argument("--reps", type=int, default=5, help="timed calls per kernel of the --kernels table")
+    ap.add_argument("--surface", action="store_true", help="the full-zone surface workload instead of the metric")
     args = ap.parse_args()
     if args.kernels:
         run_kernels(args)
+    elif args.surface:
+        run_surface(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -185,6 +185,12 @@ void mxg_solver_free(mxg_solver *s);
  * (nk*m), block steps per k (nk), final residual per vector (nk*m) */
 int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xfactor, const mxg_field *yfactor,
                     double *lambda, int *steps, double *residual);
+/* The full-zone surface of exp_blochsurf (exp_blochsurf.c:25-37, 964-1489):
+ * steps x steps k-points k = 2 pi (ix, iy) / (steps - 1) - (pi, pi), solved
+ * in waves of o.wave k-points in row order (iy outer); every wave after the
+ * first starts from the previous wave's eigenvectors.  Outputs as
+ * mxg_bloch_solve, indexed (iy * steps + ix). */
+int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, double *residual);
 /* eigenvectors of the last solved batch: wave k-points x m vectors in dense order */
 int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of

@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
             "mxg_solver_kernel_time": (I, [P, P, P, P]),
             "mxg_eps_sensitivity": (I, [I, P, I, P, P, I, P, P, P]),
             "mxg_device_ok": (I, []),
+            "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
         }
         for name, (res, args) in protos.items():
@@ -284,6 +285,17 @@ class Solver:
         check(lib().mxg_bloch_solve(self.h, nk, _ptr(xf), _ptr(yf), _ptr(lam), _ptr(steps), _ptr(res)),
               "mxg_bloch_solve")
         return lam, steps, res
+
+    def surface(self, steps: int):
+        """exp_blochsurf's full-zone grid (mxg_bloch_surface): eigenvalues
+        (steps, steps, m) indexed [iy, ix], block steps (steps, steps) and
+        residuals (steps, steps, m)."""
+        nk = steps * steps
+        lam = np.zeros((nk, self.m))
+        st = np.zeros(nk, np.int32)
+        res = np.zeros((nk, self.m))
+        check(lib().mxg_bloch_surface(self.h, steps, _ptr(lam), _ptr(st), _ptr(res)), "mxg_bloch_surface")
+        return lam.reshape(steps, steps, self.m), st.reshape(steps, steps), res.reshape(steps, steps, self.m)
 
     def eigenvectors(self) -> np.ndarray:
         a = np.zeros((self.wave, self.m, 2 * self.n * self.n), np.complex128)

@@ -88,6 +88,7 @@ struct mxg_solver {
   cudaGraphExec_t gpre[MAXL], glift[MAXL];
   long gpre_n[MAXL], glift_n[MAXL];   /* kernel launches each graph holds */
   int graphs;                          /* 1 capture and replay, 0 launch directly */
+  int restarts;                       /* warm-started waves solved again cold */
 };
 
 #define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
@@ -697,6 +698,7 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
   float ms;
   double total = 0.0;
   s->launches = 0;
+  s->restarts = 0;
   s->have_prev = 0;   /* every call starts cold; later waves of this call start warm */
   for(w = 0; w * K < nk; w++) {
     int k0 = w * K, Ka = nk - k0 < K ? nk - k0 : K;
@@ -709,12 +711,27 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
       if(s->timing) fprintf(stderr, "wave %d: cold start incl. finest-level steps %.3f s\n", w, now_s() - tc);
     }
     else {
-      /* warm start from the k-point one wave earlier (extrapolation 'n') */
+      /* warm start from the k-point one wave earlier (extrapolation 'n');
+       * its eigenvectors are divergence-free for their own Bloch phases,
+       * not for these, so they are lifted (and centred at Gamma) first */
       L_(mxk_convert(s->pe, s->Eprev, s->pe, s->E, elen(s, s->L), s->st));
+      if(s->o.center) L_(mxk_center(s->n[s->L], m, s->K, s->gamma, s->pe, s->E, s->cacc, s->st));
+      TRY(lift(s, s->L, s->pe, s->E));
       TRY(residual(s, s->L, 0));
       for(k = 0; k < K * m; k++) s->h_mu[k] = s->h_rq[k];
       TRY(upload_mu(s));
       TRY(iterate(s, s->L, s->o.max_steps, Ka));
+      /* a warm start can fail where the wanted eigenvectors of the previous
+       * wave resemble those of these k-points poorly (close to Gamma the
+       * direction of k, and with it the splitting into gradient and
+       * physical fields, turns quickly): such a wave is solved again from a
+       * cold start */
+      for(k = 0; k < Ka && converged_k(s, k); k++)
+        ;
+      if(k < Ka) {
+        s->restarts++;
+        TRY(cold_start(s, Ka));
+      }
     }
     TRY((int) cudaEventRecord(s->ev1, s->st));
     TRY((int) cudaEventSynchronize(s->ev1));
@@ -734,6 +751,7 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
   s->last_ms = total;
   if(s->timing) {
     int q;
+    if(s->restarts) fprintf(stderr, "%d warm-started wave(s) solved again cold\n", s->restarts);
     fprintf(stderr, "finest-level GPU time per phase:");
     for(q = 0; q < PH_N; q++) {
       fprintf(stderr, " %s %.3f s%s", ph_name[q], s->tph[q] / 1e3, q + 1 < PH_N ? "," : "\n");
@@ -741,6 +759,37 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
     }
   }
   return (int) cudaStreamSynchronize(s->st);
+}
+
+/* The full-zone surface of exp_blochsurf (exp_blochsurf.c:25-37, 964-1489):
+ * k = (2 pi ix / (steps - 1) - pi, 2 pi iy / (steps - 1) - pi) for
+ * ix, iy = 0 .. steps-1, solved in waves of the solver's K k-points taken in
+ * row order (iy outer, ix inner).  Wave 0 starts cold; every later wave
+ * starts from the eigenvectors of the wave before it, whose slot i holds the
+ * k-point K positions earlier on the grid -- K / steps rows lower when K is a
+ * multiple of steps -- and the first block step's Rayleigh-Ritz over
+ * [E, X] plays the part of the reference's Rayleigh extrapolation.
+ * Outputs are indexed (iy * steps + ix) as in mxg_bloch_solve. */
+int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, double *residual)
+{
+  int nk, ix, iy, e;
+  mxg_field *xf, *yf;
+  if(!s || steps < 2) return MXG_EINVAL;
+  nk = steps * steps;
+  xf = malloc(sizeof(mxg_field) * nk);
+  yf = malloc(sizeof(mxg_field) * nk);
+  if(!xf || !yf) { free(xf); free(yf); return MXG_ENOMEM; }
+  for(iy = 0; iy < steps; iy++)
+    for(ix = 0; ix < steps; ix++) {
+      const double pi = 3.14159265358979323846;
+      double xk = 2.0 * pi * ix / (steps - 1) - pi, yk = 2.0 * pi * iy / (steps - 1) - pi;
+      xf[iy * steps + ix] = cos(xk) + I * sin(xk);
+      yf[iy * steps + ix] = cos(yk) + I * sin(yk);
+    }
+  e = mxg_bloch_solve(s, nk, xf, yf, lambda, nsteps, residual);
+  free(xf);
+  free(yf);
+  return e;
 }
 
 int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host)

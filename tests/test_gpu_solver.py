@@ -55,3 +55,24 @@ def test_relative_residual_1e8(oracle):
             me = oracle.addeval_edge(n, kap, *fac[k], 0.0, 1.0, e, np.zeros_like(e))
             rr = np.linalg.norm(r) / ((lam[k, i] + 1.0) * np.linalg.norm(me))
             assert rr < 2e-8, (k, i, rr)
+
+
+def test_surface_matches_oracle(oracle):
+    """exp_blochsurf's full-zone grid (mxg_bloch_surface) on four discs: 5 x 5
+    k-points in waves of 10 (the last one partial, Gamma in a warm wave)
+    against the oracle's solves of the same k-points; 1e-8 relative."""
+    n0, L, steps, ie, m = 8, 1, 5, 6, 8
+    n = n0 << L
+    discs = [[10.0, cx, cy, 0.15] for cy in (0.25, 0.75) for cx in (0.25, 0.75)]
+    kap = oracle.disc_kappa(n, discs, 1.0)
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, wave=10, relative=1, tol=1e-9,
+                  max_nested=5, max_steps=80)
+    lam, st, res = s.surface(steps)
+    assert res[..., :ie].max() <= 1e-9
+    ks = 2 * np.pi * np.arange(steps) / (steps - 1) - np.pi
+    fac = np.array([[np.exp(1j * ks[ix]), np.exp(1j * ks[iy])] for iy in range(steps) for ix in range(steps)])
+    st_o, lam_o, _, res_o, _ = oracle.bloch_solve(kap, fac, n0=n0, L=L, ieigs=ie, m=m, method=1, max_nested=40,
+                                                  max_steps=80, tol=1e-9, relative=1, extrapolation="n", wave=1)
+    assert st_o == 0
+    got = lam.reshape(steps * steps, m)[:, :ie]
+    assert np.abs(got - lam_o[:, :ie]).max() / lam_o[:, :ie].max() < 1e-8
