@@ -648,34 +648,47 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
   const S* rowp = xk + jp * n * m;
   const S* rowc = xk + j * n * m;
   const S* rowb = bb + j * n * m;
-  auto beta_inner = [&](int ii) {
-    cx<R> sm = Store<S, R>::ld(rowm + (ii - 1) * m) + Store<S, R>::ld(rowm + ii * m)
-               + Store<S, R>::ld(rowm + (ii + 1) * m);
-    cx<R> sp = Store<S, R>::ld(rowp + (ii - 1) * m) + Store<S, R>::ld(rowp + ii * m)
-               + Store<S, R>::ld(rowp + (ii + 1) * m);
+  // an interior position's eight loads, and beta' from them; pass 1 issues
+  // the loads of two positions before it uses either, so that each thread
+  // keeps sixteen loads in flight
+  struct Ld8 {
+    cx<R> m0, m1, m2, p0, p1, p2, c, b;
+  };
+  auto load_inner = [&](int ii, Ld8& q) {
+    q.m0 = Store<S, R>::ld(rowm + (ii - 1) * m); q.m1 = Store<S, R>::ld(rowm + ii * m);
+    q.m2 = Store<S, R>::ld(rowm + (ii + 1) * m);
+    q.p0 = Store<S, R>::ld(rowp + (ii - 1) * m); q.p1 = Store<S, R>::ld(rowp + ii * m);
+    q.p2 = Store<S, R>::ld(rowp + (ii + 1) * m);
+    q.c = Store<S, R>::ld(rowc + (ii + sd) * m);
+    q.b = Store<S, R>::ld(rowb + ii * m);
+  };
+  auto beta_from = [&](const Ld8& q) {
+    cx<R> sm = q.m0 + q.m1 + q.m2, sp = q.p0 + q.p1 + q.p2;
     if (j == 0) sm = conjc(seam.yf) * sm;
     if (j == n - 1) sp = seam.yf * sp;
-    cx<R> nb = Store<S, R>::ld(rowc + (ii + sd) * m) + sm + sp;
-    return scal(inv_ac, Store<S, R>::ld(rowb + ii * m) + scal(third, nb));
+    return scal(inv_ac, q.b + scal(third, q.c + sm + sp));
+  };
+  // positions 0 and n-1, whose stencils cross the seam in i
+  auto beta_end = [&](int t) {
+    if (t == 0) return x0s[v];
+    int i = i0 + sd * t, ii = i + sd, jj = j;
+    cx<R> phz;
+    bool w = seam.wrap(ii, jj, phz);
+    return beta_at(i, w ? phz * x0s[v] : x0s[v]);
   };
   if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
   __syncthreads();
   for (int t0 = 0; t0 < n; t0 += SEG) {
     int t1 = t0 + SEG < n ? t0 + SEG : n;
-    for (int t = t0 + ty; t < t1; t += P) {
-      int i = i0 + sd * t;
-      cx<R> out;
-      if (t == 0) {
-        out = x0s[v];
-      } else if (t == n - 1) {
-        cx<R> phz;
-        int ii = i + sd, jj = j;
-        bool w = seam.wrap(ii, jj, phz);
-        out = beta_at(i, w ? phz * x0s[v] : x0s[v]);
-      } else {
-        out = beta_inner(i);
-      }
-      ring[(t & (RING - 1)) * m + v] = out;
+    for (int t = t0 + ty; t < t1; t += 2 * P) {
+      const int tb = t + P;
+      const bool hb = tb < t1;
+      const bool ina = t > 0 && t < n - 1, inb = hb && tb > 0 && tb < n - 1;
+      Ld8 qa, qb;
+      if (ina) load_inner(i0 + sd * t, qa);
+      if (inb) load_inner(i0 + sd * tb, qb);
+      ring[(t & (RING - 1)) * m + v] = ina ? beta_from(qa) : beta_end(t);
+      if (hb) ring[(tb & (RING - 1)) * m + v] = inb ? beta_from(qb) : beta_end(tb);
     }
     __syncthreads();
     for (int t = t0 + ty; t < t1; t += P) {
