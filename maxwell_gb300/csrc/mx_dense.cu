@@ -1,6 +1,7 @@
 // Batched small dense complex linear algebra in FP64 (one CTA per k-point).
-// These matrices are tiny (coarse grids of 2*8*8 = 128 edges, Ritz systems of
-// at most 3m = 48 columns), so FP64 on GB300 is affordable here; they replace
+// These matrices are small (coarse grids of 2*8*8 = 128 edges, Ritz systems
+// of at most 3m = 48 columns); the Jacobi sweeps of the Ritz step do most of
+// their rotations in FP32 and finish in FP64 (jacobi_mixed).  They replace
 // the reference's LAPACK calls (linalg.c:48-317):
 //   mxk_hpd_inverse    zpotrf + ztrsm pairs of the coarse-grid solves
 //   mxk_heev           zheev (cyclic Jacobi with Brent-Luk parallel ordering)
@@ -116,7 +117,8 @@ __global__ void k_coarse_apply(int N, int m, const MS* __restrict__ ainv, const 
 // t = sgn(tau)/(|tau| + sqrt(1+tau^2)), c = 1/sqrt(1+t^2), s = t c, and
 // V = [[c, s e], [-s conj(e), c]] on (p,q); A <- V^H A V, Z <- Z V.
 // ------------------------------------------------------------------
-__device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd, int* shi, int max_sweeps) {
+__device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd, int* shi, int max_sweeps,
+                           bool init = true) {
   // shd: 4 * (N/2 + 1) doubles of rotation data, plus 32 for reductions
   int Np = N + (N & 1);   // pad to even with a dummy index N
   int half = Np / 2;
@@ -127,12 +129,15 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
   double* red = shd + 4 * half;
   int* pp = shi;
   int* qq = shi + half;
-  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
-    int i = (int) (e % N), j = (int) (e / N);
-    AT(Zm, N, i, j) = zmk(i == j ? 1.0 : 0.0, 0.0);
-    if (i < j) AT(A, N, i, j) = zconj(AT(A, N, j, i));   // complete from the lower triangle
-    if (i == j) AT(A, N, i, i).im = 0.0;
-  }
+  // with init, Zm starts as the identity and A is completed from its lower
+  // triangle; without, A is already full and rotations accumulate onto Zm
+  if (init)
+    for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+      int i = (int) (e % N), j = (int) (e / N);
+      AT(Zm, N, i, j) = zmk(i == j ? 1.0 : 0.0, 0.0);
+      if (i < j) AT(A, N, i, j) = zconj(AT(A, N, j, i));   // complete from the lower triangle
+      if (i == j) AT(A, N, i, i).im = 0.0;
+    }
   __syncthreads();
   double fro = 0.0;
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) fro += zabs2(AT(A, N, e % N, e / N));
@@ -219,6 +224,148 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
   __syncthreads();
 }
 
+// ------------------------------------------------------------------
+// Mixed-precision Jacobi.  FP64 arithmetic on GB300 runs at a small fraction
+// of the FP32 rate and a CTA's Jacobi sweeps are bound by it, so the sweeps
+// that do the bulk of the work run in FP32: they bring the off-diagonal
+// part down to about 1e-6 of the matrix.  Their accumulated rotations Zf are
+// then made unitary to FP64 precision by one Newton-Schulz step
+// Q = Z (3I - Z^H Z) / 2, the matrix is transformed exactly in FP64,
+// A' = Q^H A Q (same eigenvalues as A), and FP64 sweeps finish A' -- one or
+// two, Jacobi converging quadratically -- accumulating into Q.
+// ------------------------------------------------------------------
+struct Cf {
+  float re, im;
+};
+
+// one cyclic Jacobi run on the FP32 copy (the same rotation as jacobi_cta)
+__device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* shi, int max_sweeps) {
+  int Np = N + (N & 1);
+  int half = Np / 2;
+  float* cs = shf;
+  float* sn = shf + half;
+  float* er = shf + 2 * half;
+  float* ei = shf + 3 * half;
+  int* pp = shi;
+  int* qq = shi + half;
+#define AF(M, i, j) (M[(size_t) (j) * N + (i)])
+  double fro = 0.0;
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+    Cf a = A[e];
+    fro += (double) a.re * a.re + (double) a.im * a.im;
+  }
+  float frof = (float) sqrt(block_sum(fro, red));
+  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+    double rotated = 0.0;
+    for (int r = 0; r < Np - 1; r++) {
+      for (int s = threadIdx.x; s < half; s += blockDim.x) {
+        int a = s == 0 ? 0 : 1 + (s - 1 + r) % (Np - 1);
+        int bpos = Np - 1 - s;
+        int b = 1 + (bpos - 1 + r) % (Np - 1);
+        int p = a < b ? a : b, q = a < b ? b : a;
+        float c = 1.0f, sv = 0.0f, xr = 1.0f, xi = 0.0f;
+        if (q < N) {
+          Cf apq = AF(A, p, q);
+          float g = sqrtf(apq.re * apq.re + apq.im * apq.im);
+          float scale = sqrtf(fabsf(AF(A, p, p).re * AF(A, q, q).re));
+          // stop where FP32 can no longer resolve the coupling
+          if (g > 1e-6f * scale && g > 1e-6f * frof) {
+            rotated += 1.0;
+            float app = AF(A, p, p).re, aqq = AF(A, q, q).re;
+            float tau = (aqq - app) / (2.0f * g);
+            float t = (tau >= 0.0f ? 1.0f : -1.0f) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+            c = 1.0f / sqrtf(1.0f + t * t);
+            sv = t * c;
+            xr = apq.re / g;
+            xi = apq.im / g;
+          }
+        }
+        pp[s] = p; qq[s] = q; cs[s] = c; sn[s] = sv; er[s] = xr; ei[s] = xi;
+      }
+      __syncthreads();
+      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
+        int s = (int) (e / N), i = (int) (e % N);
+        int p = pp[s], q = qq[s];
+        if (q >= N || sn[s] == 0.0f) continue;
+        float c = cs[s], sv = sn[s], xr = er[s], xi = ei[s];
+        Cf ap = AF(A, i, p), aq = AF(A, i, q);
+        // ap' = c ap - s conj(e) aq, aq' = s e ap + c aq
+        AF(A, i, p) = Cf{c * ap.re - sv * (xr * aq.re + xi * aq.im), c * ap.im - sv * (xr * aq.im - xi * aq.re)};
+        AF(A, i, q) = Cf{sv * (xr * ap.re - xi * ap.im) + c * aq.re, sv * (xr * ap.im + xi * ap.re) + c * aq.im};
+        Cf zp = AF(Zm, i, p), zq = AF(Zm, i, q);
+        AF(Zm, i, p) = Cf{c * zp.re - sv * (xr * zq.re + xi * zq.im), c * zp.im - sv * (xr * zq.im - xi * zq.re)};
+        AF(Zm, i, q) = Cf{sv * (xr * zp.re - xi * zp.im) + c * zq.re, sv * (xr * zp.im + xi * zp.re) + c * zq.im};
+      }
+      __syncthreads();
+      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
+        int s = (int) (e / N), j = (int) (e % N);
+        int p = pp[s], q = qq[s];
+        if (q >= N || sn[s] == 0.0f) continue;
+        float c = cs[s], sv = sn[s], xr = er[s], xi = ei[s];
+        Cf ap = AF(A, p, j), aq = AF(A, q, j);
+        // ap' = c ap - s e aq, aq' = s conj(e) ap + c aq
+        AF(A, p, j) = Cf{c * ap.re - sv * (xr * aq.re - xi * aq.im), c * ap.im - sv * (xr * aq.im + xi * aq.re)};
+        AF(A, q, j) = Cf{sv * (xr * ap.re + xi * ap.im) + c * aq.re, sv * (xr * ap.im - xi * ap.re) + c * aq.im};
+      }
+      __syncthreads();
+    }
+    if (block_sum(rotated, red) == 0.0) break;
+  }
+#undef AF
+}
+
+// C = op(X) Y for N x N complex FP64 matrices, op = conjugate transpose when cx
+__device__ void zgemm_cta(int N, double* X, bool cx, double* Y, double* C) {
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+    int i = (int) (e % N), j = (int) (e / N);
+    Z s = zmk(0.0, 0.0);
+    if (cx)
+      for (int l = 0; l < N; l++) s = zadd(s, zcmul(AT(X, N, l, i), AT(Y, N, l, j)));
+    else
+      for (int l = 0; l < N; l++) s = zadd(s, zmul(AT(X, N, i, l), AT(Y, N, l, j)));
+    AT(C, N, i, j) = s;
+  }
+  __syncthreads();
+}
+
+// Eigen-decomposition of the Hermitian A (lower triangle used; overwritten)
+// into w (ascending) and Zm.  Buffers: F (N*N complex doubles of space: the
+// FP32 copies, later Q) and G (N*N complex doubles).
+__device__ void jacobi_mixed(int N, double* A, double* Zm, double* w, double* shd, int* shi, double* F, double* G) {
+  int half = (N + (N & 1)) / 2;
+  double* red = shd + 4 * (half + 1);
+  Cf* Af = reinterpret_cast<Cf*>(F);
+  Cf* Zf = Af + (size_t) N * N;
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+    int i = (int) (e % N), j = (int) (e / N);
+    Z a = i >= j ? AT(A, N, i, j) : zconj(AT(A, N, j, i));
+    if (i == j) a.im = 0.0;
+    if (i <= j) AT(A, N, i, j) = a;   // complete the FP64 matrix as well
+    Af[e] = Cf{(float) a.re, (float) a.im};
+    Zf[e] = Cf{i == j ? 1.0f : 0.0f, 0.0f};
+  }
+  __syncthreads();
+  jacobi_f32(N, Af, Zf, reinterpret_cast<float*>(shd), red, shi, 30);
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x)
+    reinterpret_cast<Z*>(Zm)[e] = zmk((double) Zf[e].re, (double) Zf[e].im);
+  __syncthreads();
+  // Q = Z (3I - Z^H Z) / 2 into F
+  zgemm_cta(N, Zm, true, Zm, G);
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
+    int i = (int) (e % N), j = (int) (e / N);
+    Z g = reinterpret_cast<Z*>(G)[e];
+    reinterpret_cast<Z*>(G)[e] = zmk((i == j ? 1.5 : 0.0) - 0.5 * g.re, -0.5 * g.im);
+  }
+  __syncthreads();
+  zgemm_cta(N, Zm, false, G, F);
+  // A' = Q^H A Q, then the FP64 sweeps accumulate onto Q
+  zgemm_cta(N, A, false, F, G);
+  zgemm_cta(N, F, true, G, A);
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) reinterpret_cast<Z*>(Zm)[e] = reinterpret_cast<Z*>(F)[e];
+  __syncthreads();
+  jacobi_cta(N, A, Zm, w, shd, shi, 20, false);
+}
+
 __global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
   extern __shared__ double sm[];
   int half = (N + 1) / 2 + 1;
@@ -232,7 +379,7 @@ __global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
 
 // ------------------------------------------------------------------
 // Rayleigh-Ritz from Gram matrices (see mx_internal.h)
-// workspace per k: 4 * ns * ns complex doubles
+// workspace per k: 5 * ns * ns complex doubles
 // ------------------------------------------------------------------
 __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, const double* __restrict__ gm,
                                 const int* __restrict__ sel, double drop, double theta_min, double* coef,
@@ -256,12 +403,15 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
     uintptr_t p0 = reinterpret_cast<uintptr_t>(cnt + 2);
     W0 = reinterpret_cast<double*>((p0 + 15) & ~(uintptr_t) 15);
   } else {
-    W0 = work + (size_t) k * 8 * ns * ns;
+    W0 = work + (size_t) k * 10 * ns * ns;
   }
   double* W1 = W0 + 2 * ns * ns;                     // T = D R^-1
   double* W2 = W1 + 2 * ns * ns;                     // G_A T, then projected A
   double* W3 = W2 + 2 * ns * ns;                     // Jacobi eigenvectors
   double* GS = in_smem ? W3 + 2 * ns * ns : nullptr; // G_A on the selected columns
+  // work of the mixed Jacobi: W0 (free once T is formed) and GS, or in global
+  // memory a fifth matrix
+  double* GB = in_smem ? GS : W3 + 2 * ns * ns;
   if (threadIdx.x == 0) {
     int na = 0;
     for (int i = 0; i < ns; i++)
@@ -351,7 +501,7 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
     AT(W2, r, a, c) = s;
   }
   __syncthreads();
-  jacobi_cta(r, W2, W3, wv, shd, shi, 60);
+  jacobi_mixed(r, W2, W3, wv, shd, shi, W0, GB);
   // Ritz values at or below theta_min are spurious (null-space) modes and
   // are passed over, as exp_bloch2d.c:546-551 does for its coarse start
   if (threadIdx.x == 0) {
