@@ -163,7 +163,7 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
          mxk_edge_apply(n, m, K, ph, kap, -1.0, -1.0, 0, 1.0, MX_C64, x, MX_C64, b, d, st));
     TIME("afw_sweep_forward_c64", 3 * E8 * s8 + kb4 + 32.0 * nn, 2,
          mxk_edge_gs(n, m, K, ph, kap, 1.0, 1.0, 0, MX_C64, b, x, st));
-    TIME("afw_colour_forward_c64", 3 * E8 * s8 + kb4 + 32.0 * nn, 4,
+    TIME("afw_colour_forward_c64", 3 * E8 * s8 + kb4 + 32.0 * nn, 2,
          mxk_edge_gs_colour(n, m, K, ph, kap, 1.0, 1.0, 0, MX_C64, b, x, st));
     TIME("edge_restrict_c64", (E8 + 2 * E8 / 4) * s8, 1,
          mxk_edge_restrict(n / 2, m, K, ph, 1.0, MX_C64, d, bc, st));

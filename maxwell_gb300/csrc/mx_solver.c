@@ -316,14 +316,11 @@ static int edge_gs(mxg_solver *s, int l, int dir)
     if(s->npev + 2 > s->maxpev) prof_flush(s);
     cudaEventRecord(s->pev[s->npev++], s->st);
   }
-  if(s->o.smoother) {
+  if(s->o.smoother)
     e = mxk_edge_gs_colour(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
-    s->launches += 4 * (dir == 2 ? 2 : 1);
-  }
-  else {
+  else
     e = mxk_edge_gs(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
-    s->launches += 2 * (dir == 2 ? 2 : 1);
-  }
+  s->launches += 2 * (dir == 2 ? 2 : 1);
   if(timed) cudaEventRecord(s->pev[s->npev++], s->st);
   return e;
 }

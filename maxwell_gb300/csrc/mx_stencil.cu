@@ -402,11 +402,12 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
 // AFW vertex-patch smoother in four colours.  The vertices (i, j) split by
 // (i mod 2, j mod 2); two patches of one colour share no unknown, and none
 // reads an unknown the other writes (a patch writes x(i-1..i, j) and
-// y(i, j-1..j) and reads x(i-1..i, j-1..j+1), y(i-1..i+1, j-1..j)), so one
-// launch solves every patch of a colour at once: one thread per (patch,
+// y(i, j-1..j) and reads x(i-1..i, j-1..j+1), y(i-1..i+1, j-1..j)), so the
+// patches of a colour are solved concurrently, one thread per (patch,
 // vector, k-point), the same local solve as the row sweep.  A forward sweep
 // takes the colours (0,0), (1,0), (0,1), (1,1), a backward sweep the reverse
-// order.  The iterates differ from the reference's row order; both are
+// order; the two colours of one vertex-row parity share a launch
+// (k_edge_gs_rowpair).  The iterates differ from the reference's row order; both are
 // convergent splittings of the same operator, so the eigenpairs the solver
 // converges to are the same.
 // ------------------------------------------------------------------
@@ -417,16 +418,12 @@ __device__ __forceinline__ void st_edge(S* base, int n, int m, const Seam<R>& se
   Store<S, R>::st(base + ((p * n + j) * n + i) * m, v);
 }
 
+// one patch solve of the colour sweeps: vertex (i, j), k-point k, vector v
 template <typename S, typename R>
-__global__ void k_edge_gs_colour(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
-                                 const float4* __restrict__ ftab, Sc axy_s, Sc mm_s, Sc s8_s, Sc is8_s, int ci,
-                                 int cj, const S* __restrict__ b, S* x) {
-  // block (m, rows): x = vector, y = patch of the colour; grid.y = k-point
-  const int h = n / 2;
-  const int k = blockIdx.y, v = threadIdx.x;
-  const int q = blockIdx.x * blockDim.y + threadIdx.y;
-  if (q >= h * h) return;
-  const int i = 2 * (q % h) + ci, j = 2 * (q / h) + cj;
+__device__ __forceinline__ void afw_patch(int n, int m, int K, const double* __restrict__ ph, const Kap<R>& kap,
+                                          const float4* __restrict__ ftab, const Sc& axy_s, const Sc& mm_s,
+                                          const Sc& s8_s, const Sc& is8_s, int i, int j, int k, int v,
+                                          const S* __restrict__ b, S* x) {
   Lay L{n, m, K};
   S* xb = x + L.edge(k, 0, 0, 0, v);
   const S* bb = b + L.edge(k, 0, 0, 0, v);
@@ -494,6 +491,37 @@ __global__ void k_edge_gs_colour(int n, int m, int K, const double* __restrict__
     st_edge<S, R>(xb, n, m, seam, 1, i, j - 1, yb0);
     st_edge<S, R>(xb, n, m, seam, 1, i, j, yb1);
   }
+}
+
+// The colours (0, cj) and (1, cj) in one launch: a CTA per vertex row j of
+// parity cj and k-point.  The first colour is F = rev (even i forward, odd
+// i backward), the second G = 1 - F.  A patch interacts (shares unknowns or
+// reads another's) only with its left and right neighbours in the row, so
+// the CTA walks the row in chunks of P first-colour patches i = 2p + F and,
+// after a barrier, solves the second-colour patches i = 2p + F - 1 between
+// them and the previous chunk; the wrapped second-colour patch (F - 1 mod n)
+// comes last.  Every second-colour patch then runs after both neighbours
+// and before nothing that reads it, so the result is that of the two colour
+// launches, and a chunk's data are read again while still on chip.  Rows of
+// one parity neither share an unknown nor read each other's, so the rows run
+// concurrently.  Barriers make a block's global writes visible to the block.
+template <typename S, typename R>
+__global__ void k_edge_gs_rowpair(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
+                                  const float4* __restrict__ ftab, Sc axy_s, Sc mm_s, Sc s8_s, Sc is8_s, int cj,
+                                  int rev, const S* __restrict__ b, S* x) {
+  // block (m, P): x = vector, y = patch lane; grid (rows of the parity, K)
+  const int k = blockIdx.y, v = threadIdx.x, P = blockDim.y, h = n / 2;
+  const int j = 2 * blockIdx.x + cj, F = rev;
+  for (int c = 0; c < h; c += P) {
+    const int p = c + threadIdx.y;
+    if (p < h) afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, 2 * p + F, j, k, v, b, x);
+    __syncthreads();
+    if (p < h && p >= 1)
+      afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, 2 * p + F - 1, j, k, v, b, x);
+    __syncthreads();
+  }
+  if (threadIdx.y == 0)
+    afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, (F + n - 1) % n, j, k, v, b, x);
 }
 
 // ------------------------------------------------------------------
@@ -608,26 +636,31 @@ struct NIO {
 // with the new x_{i0} across the seam.  Hence
 //   x_{i_t} = sum_{d=0}^{min(t,D)} 8^-d beta'_{i_{t-d}},
 // truncated where 8^-(D+1) is below the arithmetic's precision.
-// One CTA per (row, k-point) walks its row in segments of NSEG chain
-// positions: pass 1 puts beta' of the segment into a ring in shared memory
-// (reading old values only: the row's own x is rewritten one segment at a
-// time, behind every position pass 1 still reads), pass 2 writes the
-// truncated prefix sums into x.  The new x_{i0} that the last position
-// needs is formed from old values before anything is written.
-constexpr int NSEG = 64, NRING = 128;   // ring: a power of two >= NSEG + D
-
-template <typename S, typename R, int D>
-__global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s,
-                              int j0, int jstep, int backward, const S* __restrict__ b, S* x) {
-  // FP32 rows take longer segments (fewer barrier rounds per row); the
-  // float-float and FP64 rings, twice as wide per entry, keep the shorter ones
-  constexpr int SEG = D == 8 ? 2 * NSEG : NSEG, RING = D == 8 ? 2 * NRING : NRING;
-  static_assert(RING >= SEG + D && (RING & (RING - 1)) == 0, "ring too short for the prefix depth");
+// One CTA per (row, k-point) walks its row in segments of SEG = P * LR
+// chain positions, P the block's position lanes, each lane taking a run of
+// LR consecutive positions.  Pass 1 puts beta' of a segment into a ring in
+// shared memory, reading old values only: along its run a lane keeps the
+// three values of rows j-1 and j+1 that a position needs in a sliding
+// window, so a position costs four loads.  Pass 2 writes the prefix sums
+// of a segment into x: a lane starts its run with the truncated sum and
+// continues with x_t = x_{t-1}/8 + beta'_t (the GS recurrence itself).  The
+// passes are software-pipelined: a round issues the loads of pass 1 for
+// segment s+1, runs pass 2 of segment s while they are in flight, stores
+// the betas of s+1 and ends at a barrier.  Pass 2 of s reads the ring
+// slots [t0 - D, t1) and pass 1 of s+1 writes the next SEG slots, so the
+// ring holds at least 2 SEG + D slots; pass 1 of s+1 reads the row's old x
+// at positions of s+1 and at the first of s+2, none of which pass 2 of s
+// writes.  The new x_{i0} that the last position needs is formed from old
+// values before anything is written.
+template <typename S, typename R, int D, int LR>
+__global__ void __launch_bounds__(256, 2)
+    k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s, int j0,
+                  int jstep, int backward, int rmask, const S* __restrict__ b, S* x) {
   extern __shared__ float smn[];
-  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);   // RING * m
-  cx<R>* x0s = ring + RING * m;                  // m
-  int k = blockIdx.y, v = threadIdx.x, P = blockDim.y, ty = threadIdx.y;
-  int j = j0 + blockIdx.x * jstep;
+  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);      // (rmask + 1) * m
+  cx<R>* x0s = ring + (size_t) (rmask + 1) * m;     // m
+  const int k = blockIdx.y, v = threadIdx.x, ty = threadIdx.y, SEG = blockDim.y * LR;
+  const int j = j0 + blockIdx.x * jstep;
   Lay L{n, m, K};
   Seam<R> seam = seam_load<R>(ph, K, k, n);
   NAcc<S, R> X{x + L.node(k, 0, 0, v), n, m, seam};
@@ -641,33 +674,15 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
     return scal(inv_ac, Store<S, R>::ld(bb + ((size_t) j * n + ii) * m) + scal(third, nb));
   };
   // positions 1..n-2 of the row: the rows j-1, j+1 through plain pointers,
-  // with the seam phase of the whole row when it lies across the seam
+  // with the seam phase of the whole row when it lies across the seam;
+  // position t sits at column i0 + sd t
   const S* xk = x + L.node(k, 0, 0, v);
   const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
-  const S* rowm = xk + jm * n * m;
-  const S* rowp = xk + jp * n * m;
-  const S* rowc = xk + j * n * m;
-  const S* rowb = bb + j * n * m;
-  // an interior position's eight loads, and beta' from them; pass 1 issues
-  // the loads of two positions before it uses either, so that each thread
-  // keeps sixteen loads in flight
-  struct Ld8 {
-    cx<R> m0, m1, m2, p0, p1, p2, c, b;
-  };
-  auto load_inner = [&](int ii, Ld8& q) {
-    q.m0 = Store<S, R>::ld(rowm + (ii - 1) * m); q.m1 = Store<S, R>::ld(rowm + ii * m);
-    q.m2 = Store<S, R>::ld(rowm + (ii + 1) * m);
-    q.p0 = Store<S, R>::ld(rowp + (ii - 1) * m); q.p1 = Store<S, R>::ld(rowp + ii * m);
-    q.p2 = Store<S, R>::ld(rowp + (ii + 1) * m);
-    q.c = Store<S, R>::ld(rowc + (ii + sd) * m);
-    q.b = Store<S, R>::ld(rowb + ii * m);
-  };
-  auto beta_from = [&](const Ld8& q) {
-    cx<R> sm = q.m0 + q.m1 + q.m2, sp = q.p0 + q.p1 + q.p2;
-    if (j == 0) sm = conjc(seam.yf) * sm;
-    if (j == n - 1) sp = seam.yf * sp;
-    return scal(inv_ac, q.b + scal(third, q.c + sm + sp));
-  };
+  const S* rowm = xk + ((size_t) jm * n + i0) * m;
+  const S* rowp = xk + ((size_t) jp * n + i0) * m;
+  const S* rowc = xk + ((size_t) j * n + i0) * m;
+  const S* rowb = bb + ((size_t) j * n + i0) * m;
+  const int st = sd * m;   // elements from one position to the next
   // positions 0 and n-1, whose stencils cross the seam in i
   auto beta_end = [&](int t) {
     if (t == 0) return x0s[v];
@@ -676,28 +691,68 @@ __global__ void k_node_gs_row(int n, int m, int K, const double* __restrict__ ph
     bool w = seam.wrap(ii, jj, phz);
     return beta_at(i, w ? phz * x0s[v] : x0s[v]);
   };
+  // one round: pass 1 of the run [u, ue) and pass 2 of the run [t, te)
+  auto round = [&](int t, int te, int u, int ue) {
+    cx<R> wm[LR + 2], wp[LR + 2], wc[LR], wb[LR];
+    // wm[q], wp[q]: rows j-1, j+1 at position u + q - 1; wc[q], wb[q]: the
+    // row's old x at position u + q + 1 and b at u + q
+#pragma unroll
+    for (int q = 0; q < LR + 2; q++) {
+      const int pq = u + q - 1;
+      if (pq >= 0 && pq <= ue && pq < n) {
+        wm[q] = Store<S, R>::ld(rowm + pq * st);
+        wp[q] = Store<S, R>::ld(rowp + pq * st);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < LR; q++) {
+      const int pq = u + q;
+      if (pq >= 1 && pq < ue && pq < n - 1) {
+        wc[q] = Store<S, R>::ld(rowc + (pq + 1) * st);
+        wb[q] = Store<S, R>::ld(rowb + pq * st);
+      }
+    }
+    if (t < te) {
+      cx<R> acc = czero<R>();
+      const int dmax = t < D ? t : D;
+      for (int d = dmax; d >= 1; d--)   // Horner from the farthest term
+        acc = scal(eighth, acc) + ring[((t - d) & rmask) * m + v];
+#pragma unroll
+      for (int q = 0; q < LR; q++)
+        if (t + q < te) {
+          acc = scal(eighth, acc) + ring[((t + q) & rmask) * m + v];
+          Store<S, R>::st(xr + (size_t) (i0 + sd * (t + q)) * m, acc);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < LR; q++) {
+      const int pq = u + q;
+      if (pq < ue) {
+        cx<R> be;
+        if (pq >= 1 && pq < n - 1) {
+          cx<R> sm = wm[q] + wm[q + 1] + wm[q + 2], sp = wp[q] + wp[q + 1] + wp[q + 2];
+          if (j == 0) sm = conjc(seam.yf) * sm;
+          if (j == n - 1) sp = seam.yf * sp;
+          be = scal(inv_ac, wb[q] + scal(third, wc[q] + sm + sp));
+        } else {
+          be = beta_end(pq);
+        }
+        ring[(pq & rmask) * m + v] = be;
+      }
+    }
+  };
   if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
   __syncthreads();
+  const int r0 = ty * LR;
+  {
+    const int u1 = SEG < n ? SEG : n;
+    round(0, 0, r0, r0 + LR < u1 ? r0 + LR : u1);
+  }
+  __syncthreads();
   for (int t0 = 0; t0 < n; t0 += SEG) {
-    int t1 = t0 + SEG < n ? t0 + SEG : n;
-    for (int t = t0 + ty; t < t1; t += 2 * P) {
-      const int tb = t + P;
-      const bool hb = tb < t1;
-      const bool ina = t > 0 && t < n - 1, inb = hb && tb > 0 && tb < n - 1;
-      Ld8 qa, qb;
-      if (ina) load_inner(i0 + sd * t, qa);
-      if (inb) load_inner(i0 + sd * tb, qb);
-      ring[(t & (RING - 1)) * m + v] = ina ? beta_from(qa) : beta_end(t);
-      if (hb) ring[(tb & (RING - 1)) * m + v] = inb ? beta_from(qb) : beta_end(tb);
-    }
-    __syncthreads();
-    for (int t = t0 + ty; t < t1; t += P) {
-      cx<R> acc = czero<R>();
-      int dmax = t < D ? t : D;
-      for (int d = dmax; d >= 0; d--)   // Horner from the farthest term
-        acc = scal(eighth, acc) + ring[((t - d) & (RING - 1)) * m + v];
-      Store<S, R>::st(xr + (size_t) (i0 + sd * t) * m, acc);
-    }
+    const int t1 = t0 + SEG < n ? t0 + SEG : n, u1 = t1 + SEG < n ? t1 + SEG : n;
+    const int t = t0 + r0, u = t1 + r0;
+    round(t, t + LR < t1 ? t + LR : t1, u, u + LR < u1 ? u + LR : u1);
     __syncthreads();
   }
 }
@@ -995,18 +1050,6 @@ extern "C" size_t mxk_elem_size(int prec) { return prec == MX_C64 ? 8 : 16; }
    : (int) cudaErrorInvalidValue)
 
 template <typename S, typename R>
-static int L_edge_gs_colour(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha, double beta,
-                            int ci, int cj, const void* b, void* x, cudaStream_t st) {
-  const float4* ftab = (sizeof(R) == 4 && kap.afw && kap.afw_alpha == alpha && kap.afw_beta == beta)
-                           ? (const float4*) kap.afw : nullptr;
-  size_t patches = (size_t) (n / 2) * (n / 2);
-  k_edge_gs_colour<S, R><<<grd2(patches, m, K), blk2(m), 0, st>>>(
-      n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
-      make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), ci, cj, (const S*) b, (S*) x);
-  MX_CHECK_LAUNCH();
-  return 0;
-}
-template <typename S, typename R>
 static int L_edge_gs_rows(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
                           double beta, int j0, int jstep, int nrows, int backward, const void* b,
                           void* x, cudaStream_t st) {
@@ -1045,26 +1088,28 @@ static int L_node_apply(int n, int m, int K, const double* ph, double alpha, dou
   MX_CHECK_LAUNCH();
   return 0;
 }
+template <typename S, typename R, int D, int LR>
+static int L_node_gs_rows_d(int n, int m, int K, const double* ph, double alpha, int j0, int jstep, int nrows,
+                            int backward, const void* b, void* x, cudaStream_t st) {
+  dim3 g(nrows, K), b2 = blk2(m);
+  int ring = 1;
+  while (ring < 2 * (int) b2.y * LR + D) ring <<= 1;
+  size_t smem = (size_t) (ring + 1) * m * sizeof(cx<R>);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_node_gs_row<S, R, D, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  k_node_gs_row<S, R, D, LR><<<g, b2, smem, st>>>(n, m, K, ph, make_sc(3.0 / (8.0 * alpha)), make_sc(alpha / 3.0),
+                                                   j0, jstep, backward, ring - 1, (const S*) b, (S*) x);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+// 8^-(D+1) below the unit roundoff: D = 8 for FP32, 18 for FP64 and float-float
 template <typename S, typename R>
 static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, int j0, int jstep,
                           int nrows, int backward, const void* b, void* x, cudaStream_t st) {
-  dim3 g(nrows, K), b2 = blk2(m);
-  size_t smem = (size_t) ((sizeof(R) == 4 ? 2 * NRING : NRING) + 1) * m * sizeof(cx<R>);
-  Sc inv_ac = make_sc(3.0 / (8.0 * alpha)), third = make_sc(alpha / 3.0);
-  // 8^-(D+1) below the unit roundoff: D = 8 for FP32, 18 for FP64 and float-float
-  if (sizeof(R) == 4) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_node_gs_row<S, R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    k_node_gs_row<S, R, 8><<<g, b2, smem, st>>>(n, m, K, ph, inv_ac, third, j0, jstep, backward, (const S*) b,
-                                                (S*) x);
-  } else {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_node_gs_row<S, R, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    k_node_gs_row<S, R, 18><<<g, b2, smem, st>>>(n, m, K, ph, inv_ac, third, j0, jstep, backward, (const S*) b,
-                                                 (S*) x);
-  }
-  MX_CHECK_LAUNCH();
-  return 0;
+  if constexpr (sizeof(R) == 4)
+    return L_node_gs_rows_d<S, R, 8, 7>(n, m, K, ph, alpha, j0, jstep, nrows, backward, b, x, st);
+  else
+    return L_node_gs_rows_d<S, R, 18, 3>(n, m, K, ph, alpha, j0, jstep, nrows, backward, b, x, st);
 }
 template <typename S, typename R>
 static int L_node_prolong(int nc, int m, int K, const double* ph, double alpha, const void* c, void* f,
@@ -1159,22 +1204,31 @@ extern "C" int mxk_edge_gs(int n, int m, int K, const double* ph, mxk_kappa kap,
   return 0;
 }
 
+template <typename S, typename R>
+static int L_edge_gs_rowpair(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha, double beta,
+                             int cj, int rev, const void* b, void* x, cudaStream_t st) {
+  const float4* ftab = (sizeof(R) == 4 && kap.afw && kap.afw_alpha == alpha && kap.afw_beta == beta)
+                           ? (const float4*) kap.afw : nullptr;
+  k_edge_gs_rowpair<S, R><<<dim3(n / 2, K), blk2(m), 0, st>>>(
+      n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
+      make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), cj, rev, (const S*) b, (S*) x);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
 extern "C" int mxk_edge_gs_colour(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
                                   double beta, int dir, int prec, const void* b, void* x, mx_stream s) {
-  static const int order[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
   cudaStream_t st = (cudaStream_t) s;
   int e;
   if (n < 2 || (n & 1) || m < 1 || m > 256) return (int) cudaErrorInvalidValue;
+  // forward: colours (0,0), (1,0) in one row-pair launch, then (0,1),
+  // (1,1); backward: the four in reverse order
   if (dir == 0 || dir == 2)
-    for (int c = 0; c < 4; c++)
-      if ((e = MX_BY_PREC(prec, L_edge_gs_colour, n, m, K, ph, kap, alpha, beta, order[c][0], order[c][1], b, x,
-                          st)))
-        return e;
+    for (int cj = 0; cj < 2; cj++)
+      if ((e = MX_BY_PREC(prec, L_edge_gs_rowpair, n, m, K, ph, kap, alpha, beta, cj, 0, b, x, st))) return e;
   if (dir == 1 || dir == 2)
-    for (int c = 3; c >= 0; c--)
-      if ((e = MX_BY_PREC(prec, L_edge_gs_colour, n, m, K, ph, kap, alpha, beta, order[c][0], order[c][1], b, x,
-                          st)))
-        return e;
+    for (int cj = 1; cj >= 0; cj--)
+      if ((e = MX_BY_PREC(prec, L_edge_gs_rowpair, n, m, K, ph, kap, alpha, beta, cj, 1, b, x, st))) return e;
   return 0;
 }
 

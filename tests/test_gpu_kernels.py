@@ -79,22 +79,24 @@ def test_afw_smoother(oracle, setup, prec, direction):
     assert rel(ex.get(), want) < (1e-11 if prec == mx.C128 else 1e-4)
 
 
-@pytest.mark.parametrize("n", [16, 80])
+@pytest.mark.parametrize("n, m, prec", [(16, 4, mx.C64), (80, 4, mx.C64), (256, 16, mx.C64), (128, 16, mx.C128),
+                                         (128, 16, mx.CDD)])
 @pytest.mark.parametrize("direction", [0, 1, 2])
-def test_node_gs_even_block(oracle, n, direction):
-    """Node Gauss-Seidel on c64 blocks with an even number of vectors (the
-    kernel that stages row segments in shared memory), one segment (n = 16)
-    and several with a partial last one (n = 80), against the oracle."""
+def test_node_gs_even_block(oracle, n, m, prec, direction):
+    """Node Gauss-Seidel against the oracle: a row in one segment (n = 16,
+    80 at 4 vectors) and in several with a partial last one (n = 256 at 16
+    c64 vectors: segments of 112 positions; n = 128 at 16 FP64 or
+    float-float vectors: segments of 48)."""
     rng = np.random.default_rng(5)
-    K, m = 3, 4
+    K = 3
     g = mx.Grid(n, K, None, FACTORS)
     v_, w_ = cv(rng, K, m, n * n), cv(rng, K, m, n * n)
-    nv, nw = mx.Node(g, m, mx.C64, v_), mx.Node(g, m, mx.C64, w_)
+    nv, nw = mx.Node(g, m, prec, v_), mx.Node(g, m, prec, w_)
     fn = [mx.lib().gsforward_node2d_gpu, mx.lib().gsbackward_node2d_gpu, mx.lib().gssymm_node2d_gpu][direction]
     mx.check(fn(mx.fz(1.0), nv.h, nw.h))
     want = np.array([[oracle.gs_node(n, *FACTORS[k], 1.0, direction, v_[k, i], w_[k, i]) for i in range(m)]
                      for k in range(K)])
-    assert rel(nw.get(), want) < 2e-5
+    assert rel(nw.get(), want) < (2e-5 if prec == mx.C64 else 1e-11)
 
 
 @pytest.mark.parametrize("prec", [mx.C128, mx.CDD, mx.C64])
