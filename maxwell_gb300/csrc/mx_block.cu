@@ -631,12 +631,13 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
 // entries between a c64 column s_i and an E column e_j take the residual
 // form theta_j s_i^H M e_j + s_i^H r_j.  One CTA of G2T threads takes a chunk
 // of sites of one k-point, in tiles of G2S sites staged in shared memory:
-//   threads 0..255   the FP32 entries: thread (tx, ty) owns the entry
-//                    (bi*m + ty, bj*m + tx) of every block pair bi > bj, so
-//                    its operands are shared along rows and columns, plus a
-//                    share of the lower triangles of the diagonal blocks
-//                    bi = bj >= 1;
-//   threads 256..527 the E-E entries (lower triangle, <= 136), two threads
+//   threads 0..287   the FP32 entries, one 2x2 tile of entries per thread:
+//                    the 8x8 tiles of each block pair bi > bj (threads
+//                    0..191) and the lower-triangle tiles of the diagonal
+//                    blocks bi = bj >= 1 (threads 192..263); a tile loads
+//                    its two row and two column operands once per site and
+//                    accumulates the four entries by FMA;
+//   threads 288..559 the E-E entries (lower triangle, <= 136), two threads
 //                    per entry on alternate sites of a tile, accumulated as
 //                    compensated FP32 sums of exact products (TwoProd by
 //                    FMA, TwoSum; the low parts of E enter through the
@@ -644,10 +645,10 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
 //                    precision like float-float arithmetic at half its cost.
 // Partial sums per CTA go to scratch in the layout of k_block_gram.
 // ------------------------------------------------------------------
-constexpr int G2T = 544;         // 17 warps
+constexpr int G2F = 288;         // FP32 role: 9 warps, 264 tiles
+constexpr int G2T = G2F + 288;   // + E-E role: 9 warps, 272 threads used
 constexpr int G2S = 16;          // sites per tile
 constexpr int G2MAXO = 3;        // off-diagonal block pairs (nb <= 3)
-constexpr int G2MAXD = 2;        // diagonal-block entries per FP32 thread
 
 __device__ __forceinline__ void tri_index(int e, int& i, int& j) {
   i = (int) ((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
@@ -673,35 +674,36 @@ __global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
   const bool use_r = a.resid != nullptr;
 
   // ---- roles ----
-  // block pairs bi > bj in a fixed order; loops over them are unrolled so
-  // that the per-thread entry lists stay in registers
+  // FP32 tile of this thread: block row tbi, block column tbj, tile (ti, tj)
+  // of the block's 8x8 tiles; rows r0, r1 and columns c0, c1 of the Gram
+  // matrix (a row or column past the block repeats the first, unused)
   constexpr int PBI[G2MAXO] = {1, 2, 2}, PBJ[G2MAXO] = {0, 0, 1};
-  const bool frole = tid < 256;
-  const int tx = tid & 15, ty = (tid >> 4) & 15;
-  const bool otile = frole && tx < m && ty < m;
-  int dli[G2MAXD], dlj[G2MAXD];
-  bool dact[G2MAXD];
-  // accumulators: FP32 threads use all of acc (3 off-diagonal entries, then
-  // 2 diagonal ones, 4 floats each), E-E threads the first 8 (A, M as
-  // compensated sums)
-  float acc[4 * (G2MAXO + G2MAXD)];
-  const int ndiag = (nb - 1) * ment;
-#pragma unroll
-  for (int q = 0; q < G2MAXD; q++) {
-    int e = tid + 256 * q, i = 0, j = 0;
-    dact[q] = frole && e < ndiag;
-    if (dact[q]) tri_index(e % ment, i, j);
-    int blk = dact[q] ? 1 + e / ment : 0;
-    dli[q] = blk * m + i;
-    dlj[q] = blk * m + j;
+  int tbi = nb, tbj = 0, ti = 0, tj = 0;
+  if (tid < 64 * G2MAXO) {
+    tbi = PBI[tid >> 6];
+    tbj = PBJ[tid >> 6];
+    ti = (tid & 63) >> 3;
+    tj = tid & 7;
+  } else if (tid < 64 * G2MAXO + 72) {
+    const int e = tid - 64 * G2MAXO;
+    tbi = tbj = 1 + e / 36;
+    tri_index(e % 36, ti, tj);
   }
-  const int u = tid - 256;
+  const bool ftile = tbi < nb && 2 * ti < m && 2 * tj < m;
+  const bool rmode = use_r && tbj == 0;
+  const int r0 = tbi * m + 2 * ti, c0 = tbj * m + 2 * tj;
+  const int r1 = 2 * ti + 1 < m ? r0 + 1 : r0, c1 = 2 * tj + 1 < m ? c0 + 1 : c0;
+  // accumulators: an FP32 tile uses all of acc (entry (r_a, c_b) at
+  // 4 (2a + b): A re, A im, M re, M im), E-E threads the first 8 (A, M as
+  // compensated sums)
+  float acc[16];
+  const int u = tid - G2F;
   const bool drole = u >= 0 && (u >> 1) < ment;
   const int half = u & 1;
   int ei = 0, ej = 0;
   if (drole) tri_index(u >> 1, ei, ej);
 #pragma unroll
-  for (int q = 0; q < 4 * (G2MAXO + G2MAXD); q++) acc[q] = 0.f;
+  for (int q = 0; q < 16; q++) acc[q] = 0.f;
   float* const eacc_a = acc;
   float* const eacc_m = acc + 4;
 
@@ -778,28 +780,44 @@ __global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
       }
     __syncthreads();
     // ---- accumulation ----
-    if (frole) {
+    if (ftile) {
       for (int ts = 0; ts < nts; ts++) {
         const cx<float>* I = fi + ts * 3 * ns;
         const cx<float>* J = fj + ts * 3 * ns;
         const cx<float>* Rr = fr + ts * 2 * m;
+        const cx<float> xr[2] = {I[ns + r0], I[ns + r1]}, yr[2] = {I[2 * ns + r0], I[2 * ns + r1]};
+        const cx<float> cr[2] = {I[r0], I[r1]};
 #pragma unroll
-        for (int q = 0; q < G2MAXO; q++) {
-          if (!otile || PBI[q] >= nb) continue;
-          int i = PBI[q] * m + ty, j = PBJ[q] * m + tx;
-          cx<float> xi = I[ns + i], yi = I[2 * ns + i];
-          cx<float> mm = conjc(xi) * J[ns + j] + conjc(yi) * J[2 * ns + j];
-          cx<float> aa = j < m && use_r ? conjc(xi) * Rr[j] + conjc(yi) * Rr[m + j] : conjc(I[i]) * J[j];
-          acc[4 * q] += aa.re; acc[4 * q + 1] += aa.im; acc[4 * q + 2] += mm.re; acc[4 * q + 3] += mm.im;
-        }
+        for (int bq = 0; bq < 2; bq++) {
+          const int c = bq ? c1 : c0;
+          const cx<float> mx = J[ns + c], my = J[2 * ns + c];
+          cx<float> ka = mkc(0.f, 0.f), kb = mkc(0.f, 0.f);
+          if (rmode) {
+            ka = Rr[c];
+            kb = Rr[m + c];
+          } else {
+            ka = J[c];
+          }
 #pragma unroll
-        for (int q = 0; q < G2MAXD; q++) {
-          if (!dact[q]) continue;
-          int i = dli[q], j = dlj[q];
-          cx<float> mm = conjc(I[ns + i]) * J[ns + j] + conjc(I[2 * ns + i]) * J[2 * ns + j];
-          cx<float> aa = conjc(I[i]) * J[j];
-          float* d = acc + 4 * (G2MAXO + q);
-          d[0] += aa.re; d[1] += aa.im; d[2] += mm.re; d[3] += mm.im;
+          for (int aq = 0; aq < 2; aq++) {
+            float* d = acc + 4 * (2 * aq + bq);
+            // M: conj(x) Mx + conj(y) My
+            d[2] = fmaf(xr[aq].re, mx.re, d[2]); d[2] = fmaf(xr[aq].im, mx.im, d[2]);
+            d[2] = fmaf(yr[aq].re, my.re, d[2]); d[2] = fmaf(yr[aq].im, my.im, d[2]);
+            d[3] = fmaf(xr[aq].re, mx.im, d[3]); d[3] = fmaf(-xr[aq].im, mx.re, d[3]);
+            d[3] = fmaf(yr[aq].re, my.im, d[3]); d[3] = fmaf(-yr[aq].im, my.re, d[3]);
+            if (rmode) {
+              // A as s^H r: conj(x) rx + conj(y) ry
+              d[0] = fmaf(xr[aq].re, ka.re, d[0]); d[0] = fmaf(xr[aq].im, ka.im, d[0]);
+              d[0] = fmaf(yr[aq].re, kb.re, d[0]); d[0] = fmaf(yr[aq].im, kb.im, d[0]);
+              d[1] = fmaf(xr[aq].re, ka.im, d[1]); d[1] = fmaf(-xr[aq].im, ka.re, d[1]);
+              d[1] = fmaf(yr[aq].re, kb.im, d[1]); d[1] = fmaf(-yr[aq].im, kb.re, d[1]);
+            } else {
+              // A: conj(curl) kappa curl
+              d[0] = fmaf(cr[aq].re, ka.re, d[0]); d[0] = fmaf(cr[aq].im, ka.im, d[0]);
+              d[1] = fmaf(cr[aq].re, ka.im, d[1]); d[1] = fmaf(-cr[aq].im, ka.re, d[1]);
+            }
+          }
         }
       }
     } else if (drole) {
@@ -829,13 +847,17 @@ __global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
     out[(size_t) e * 4 + 2] = mr;
     out[(size_t) e * 4 + 3] = mi;
   };
+  if (ftile)
 #pragma unroll
-  for (int q = 0; q < G2MAXO; q++)
-    if (otile && PBI[q] < nb) put(PBI[q] * m + ty, PBJ[q] * m + tx, acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+    for (int aq = 0; aq < 2; aq++)
 #pragma unroll
-  for (int q = 0; q < G2MAXD; q++)
-    if (dact[q]) put(dli[q], dlj[q], acc[4 * (G2MAXO + q)], acc[4 * (G2MAXO + q) + 1], acc[4 * (G2MAXO + q) + 2],
-                     acc[4 * (G2MAXO + q) + 3]);
+      for (int bq = 0; bq < 2; bq++) {
+        const int r = aq ? r1 : r0, c = bq ? c1 : c0;
+        // skip the repeated row or column and the upper entry of a diagonal tile
+        if ((aq && r1 == r0) || (bq && c1 == c0) || (tbi == tbj && r - tbi * m < c - tbj * m)) continue;
+        const float* d = acc + 4 * (2 * aq + bq);
+        put(r, c, d[0], d[1], d[2], d[3]);
+      }
   // the two halves of every E-E entry meet in shared memory
   double* xch = reinterpret_cast<double*>(sm2);     // [ment][4]
   if (drole && half == 1) {

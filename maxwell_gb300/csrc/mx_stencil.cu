@@ -636,124 +636,198 @@ struct NIO {
 // with the new x_{i0} across the seam.  Hence
 //   x_{i_t} = sum_{d=0}^{min(t,D)} 8^-d beta'_{i_{t-d}},
 // truncated where 8^-(D+1) is below the arithmetic's precision.
-// One CTA per (row, k-point) walks its row in segments of SEG = P * LR
-// chain positions, P the block's position lanes, each lane taking a run of
-// LR consecutive positions.  Pass 1 puts beta' of a segment into a ring in
-// shared memory, reading old values only: along its run a lane keeps the
-// three values of rows j-1 and j+1 that a position needs in a sliding
-// window, so a position costs four loads.  Pass 2 writes the prefix sums
-// of a segment into x: a lane starts its run with the truncated sum and
-// continues with x_t = x_{t-1}/8 + beta'_t (the GS recurrence itself).  The
-// passes are software-pipelined: a round issues the loads of pass 1 for
-// segment s+1, runs pass 2 of segment s while they are in flight, stores
-// the betas of s+1 and ends at a barrier.  Pass 2 of s reads the ring
-// slots [t0 - D, t1) and pass 1 of s+1 writes the next SEG slots, so the
-// ring holds at least 2 SEG + D slots; pass 1 of s+1 reads the row's old x
-// at positions of s+1 and at the first of s+2, none of which pass 2 of s
-// writes.  The new x_{i0} that the last position needs is formed from old
-// values before anything is written.
-template <typename S, typename R, int D, int LR>
-__global__ void __launch_bounds__(256, 2)
-    k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s, int j0,
-                  int jstep, int backward, int rmask, const S* __restrict__ b, S* x) {
-  extern __shared__ float smn[];
-  cx<R>* ring = reinterpret_cast<cx<R>*>(smn);      // (rmask + 1) * m
-  cx<R>* x0s = ring + (size_t) (rmask + 1) * m;     // m
-  const int k = blockIdx.y, v = threadIdx.x, ty = threadIdx.y, SEG = blockDim.y * LR;
-  const int j = j0 + blockIdx.x * jstep;
-  Lay L{n, m, K};
-  Seam<R> seam = seam_load<R>(ph, K, k, n);
-  NAcc<S, R> X{x + L.node(k, 0, 0, v), n, m, seam};
-  S* xr = x + L.node(k, j, 0, v);
-  const S* bb = b + L.node(k, 0, 0, v);
-  const int sd = backward ? -1 : 1, i0 = backward ? n - 1 : 0;
-  const R inv_ac = sget<R>(inv_ac_s), third = sget<R>(third_s), eighth = rc<R>(0.125f);
-  auto beta_at = [&](int ii, cx<R> next) {
+// A lane takes runs of LR consecutive chain positions.  Pass 1 puts beta'
+// of its run into a ring in shared memory, reading old values only: along
+// the run the lane keeps the three values of rows j-1 and j+1 that a
+// position needs in a sliding window, so a position costs four loads.
+// Pass 2 writes the prefix sums of a run into x: the lane starts it with
+// the truncated sum over the ring and continues with x_t = x_{t-1}/8 +
+// beta'_t (the GS recurrence itself).  Pass 1 of a run reads the row's old
+// x at the run's positions and the next one only, so runs whose pass 2
+// is done may lie behind it.  The new x_{i0} that the last position needs
+// is formed from old values before anything is written.
+
+// the row j of k-point k, vector v, for the sweep; position t sits at
+// column i0 + sd t
+template <typename S, typename R>
+struct GsRow {
+  int n, m, j, sd, i0, st;
+  Seam<R> seam;
+  NAcc<S, R> X;
+  const S *bb, *rowm, *rowp, *rowc, *rowb;
+  S* xr;
+  R inv_ac, third;
+  __device__ GsRow(int n_, int m_, int K, int k, int v, int j_, int backward, const double* ph, Sc inv_ac_s,
+                   Sc third_s, const S* b, S* x)
+      : n(n_), m(m_), j(j_), sd(backward ? -1 : 1), i0(backward ? n_ - 1 : 0), st((backward ? -1 : 1) * m_),
+        seam(seam_load<R>(ph, K, k, n_)), X{nullptr, n_, m_, seam}, inv_ac(sget<R>(inv_ac_s)),
+        third(sget<R>(third_s)) {
+    Lay L{n, m, K};
+    const S* xk = x + L.node(k, 0, 0, v);
+    X.base = xk;
+    bb = b + L.node(k, 0, 0, v);
+    xr = x + L.node(k, j, 0, v);
+    // rows j-1, j+1 through plain pointers, with the seam phase of the whole
+    // row applied to the sums when it lies across the seam
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    rowm = xk + ((size_t) jm * n + i0) * m;
+    rowp = xk + ((size_t) jp * n + i0) * m;
+    rowc = xk + ((size_t) j * n + i0) * m;
+    rowb = bb + ((size_t) j * n + i0) * m;
+  }
+  __device__ cx<R> beta_at(int ii, cx<R> next) const {
     cx<R> nb = next + X(ii - 1, j - 1) + X(ii, j - 1) + X(ii + 1, j - 1) + X(ii - 1, j + 1) + X(ii, j + 1)
                + X(ii + 1, j + 1);
     return scal(inv_ac, Store<S, R>::ld(bb + ((size_t) j * n + ii) * m) + scal(third, nb));
-  };
-  // positions 1..n-2 of the row: the rows j-1, j+1 through plain pointers,
-  // with the seam phase of the whole row when it lies across the seam;
-  // position t sits at column i0 + sd t
-  const S* xk = x + L.node(k, 0, 0, v);
-  const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
-  const S* rowm = xk + ((size_t) jm * n + i0) * m;
-  const S* rowp = xk + ((size_t) jp * n + i0) * m;
-  const S* rowc = xk + ((size_t) j * n + i0) * m;
-  const S* rowb = bb + ((size_t) j * n + i0) * m;
-  const int st = sd * m;   // elements from one position to the next
-  // positions 0 and n-1, whose stencils cross the seam in i
-  auto beta_end = [&](int t) {
-    if (t == 0) return x0s[v];
+  }
+  // the new x_{i0}, from old values only
+  __device__ cx<R> x0() const { return beta_at(i0, X(i0 + sd, j)) + scal(rc<R>(0.125f), X(i0 - sd, j)); }
+  // beta' at positions 0 and n-1, whose stencils cross the seam in i
+  __device__ cx<R> beta_end(int t, cx<R> x0v) const {
+    if (t == 0) return x0v;
     int i = i0 + sd * t, ii = i + sd, jj = j;
     cx<R> phz;
     bool w = seam.wrap(ii, jj, phz);
-    return beta_at(i, w ? phz * x0s[v] : x0s[v]);
-  };
-  // one round: pass 1 of the run [u, ue) and pass 2 of the run [t, te)
-  auto round = [&](int t, int te, int u, int ue) {
+    return beta_at(i, w ? phz * x0v : x0v);
+  }
+  // pass 1 of the run [u, ue) (ue <= u + LR): the window loads ...
+  template <int LR>
+  struct Win {
     cx<R> wm[LR + 2], wp[LR + 2], wc[LR], wb[LR];
+  };
+  template <int LR>
+  __device__ __forceinline__ void load(int u, int ue, Win<LR>& w) const {
     // wm[q], wp[q]: rows j-1, j+1 at position u + q - 1; wc[q], wb[q]: the
     // row's old x at position u + q + 1 and b at u + q
 #pragma unroll
     for (int q = 0; q < LR + 2; q++) {
       const int pq = u + q - 1;
       if (pq >= 0 && pq <= ue && pq < n) {
-        wm[q] = Store<S, R>::ld(rowm + pq * st);
-        wp[q] = Store<S, R>::ld(rowp + pq * st);
+        w.wm[q] = Store<S, R>::ld(rowm + pq * st);
+        w.wp[q] = Store<S, R>::ld(rowp + pq * st);
       }
     }
 #pragma unroll
     for (int q = 0; q < LR; q++) {
       const int pq = u + q;
       if (pq >= 1 && pq < ue && pq < n - 1) {
-        wc[q] = Store<S, R>::ld(rowc + (pq + 1) * st);
-        wb[q] = Store<S, R>::ld(rowb + pq * st);
+        w.wc[q] = Store<S, R>::ld(rowc + (pq + 1) * st);
+        w.wb[q] = Store<S, R>::ld(rowb + pq * st);
       }
     }
-    if (t < te) {
-      cx<R> acc = czero<R>();
-      const int dmax = t < D ? t : D;
-      for (int d = dmax; d >= 1; d--)   // Horner from the farthest term
-        acc = scal(eighth, acc) + ring[((t - d) & rmask) * m + v];
-#pragma unroll
-      for (int q = 0; q < LR; q++)
-        if (t + q < te) {
-          acc = scal(eighth, acc) + ring[((t + q) & rmask) * m + v];
-          Store<S, R>::st(xr + (size_t) (i0 + sd * (t + q)) * m, acc);
-        }
-    }
+  }
+  // ... and the betas of the run into the ring slots (pos & rmask) * m
+  template <int LR>
+  __device__ __forceinline__ void betas(int u, int ue, const Win<LR>& w, cx<R>* ring, int rmask,
+                                        cx<R> x0v) const {
 #pragma unroll
     for (int q = 0; q < LR; q++) {
       const int pq = u + q;
       if (pq < ue) {
         cx<R> be;
         if (pq >= 1 && pq < n - 1) {
-          cx<R> sm = wm[q] + wm[q + 1] + wm[q + 2], sp = wp[q] + wp[q + 1] + wp[q + 2];
+          cx<R> sm = w.wm[q] + w.wm[q + 1] + w.wm[q + 2], sp = w.wp[q] + w.wp[q + 1] + w.wp[q + 2];
           if (j == 0) sm = conjc(seam.yf) * sm;
           if (j == n - 1) sp = seam.yf * sp;
-          be = scal(inv_ac, wb[q] + scal(third, wc[q] + sm + sp));
+          be = scal(inv_ac, w.wb[q] + scal(third, w.wc[q] + sm + sp));
         } else {
-          be = beta_end(pq);
+          be = beta_end(pq, x0v);
         }
-        ring[(pq & rmask) * m + v] = be;
+        ring[(pq & rmask) * m] = be;
       }
     }
-  };
-  if (ty == 0) x0s[v] = beta_at(i0, X(i0 + sd, j)) + scal(eighth, X(i0 - sd, j));
+  }
+  // pass 2 of the run [t, te) from the ring
+  template <int D, int LR>
+  __device__ __forceinline__ void prefix(int t, int te, const cx<R>* ring, int rmask) const {
+    if (t >= te) return;
+    const R eighth = rc<R>(0.125f);
+    cx<R> acc = czero<R>();
+    const int dmax = t < D ? t : D;
+    for (int d = dmax; d >= 1; d--)   // Horner from the farthest term
+      acc = scal(eighth, acc) + ring[((t - d) & rmask) * m];
+#pragma unroll
+    for (int q = 0; q < LR; q++)
+      if (t + q < te) {
+        acc = scal(eighth, acc) + ring[((t + q) & rmask) * m];
+        Store<S, R>::st(xr + (size_t) (i0 + sd * (t + q)) * m, acc);
+      }
+  }
+};
+
+// One CTA per (row, k-point): P position lanes walk the row in segments of
+// SEG = P LR positions.  The passes are software-pipelined: a round issues
+// the loads of pass 1 for segment s+1, runs pass 2 of segment s while they
+// are in flight, stores the betas of s+1 and ends at a barrier.  Pass 2 of
+// s reads the ring slots [t0 - D, t1) and pass 1 of s+1 writes the next
+// SEG slots, so the ring holds at least 2 SEG + D slots.  Used for the
+// single rows 0 and n-1, where one row per k-point leaves the GPU idle
+// otherwise.
+template <typename S, typename R, int D, int LR>
+__global__ void __launch_bounds__(256, 2)
+    k_node_gs_row(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s, int j0,
+                  int jstep, int backward, int rmask, const S* __restrict__ b, S* x) {
+  extern __shared__ float smn[];
+  const int k = blockIdx.y, v = threadIdx.x, ty = threadIdx.y, SEG = blockDim.y * LR;
+  cx<R>* ring = reinterpret_cast<cx<R>*>(smn) + v;           // (rmask + 1) * m
+  cx<R>* x0s = reinterpret_cast<cx<R>*>(smn) + (size_t) (rmask + 1) * m;   // m
+  const GsRow<S, R> row(n, m, K, k, v, j0 + blockIdx.x * jstep, backward, ph, inv_ac_s, third_s, b, x);
+  using W = typename GsRow<S, R>::template Win<LR>;
+  if (ty == 0) x0s[v] = row.x0();
   __syncthreads();
+  const cx<R> x0v = x0s[v];
   const int r0 = ty * LR;
   {
-    const int u1 = SEG < n ? SEG : n;
-    round(0, 0, r0, r0 + LR < u1 ? r0 + LR : u1);
+    const int u1 = SEG < n ? SEG : n, ue = r0 + LR < u1 ? r0 + LR : u1;
+    W w;
+    row.load<LR>(r0, ue, w);
+    row.betas<LR>(r0, ue, w, ring, rmask, x0v);
   }
   __syncthreads();
   for (int t0 = 0; t0 < n; t0 += SEG) {
     const int t1 = t0 + SEG < n ? t0 + SEG : n, u1 = t1 + SEG < n ? t1 + SEG : n;
-    const int t = t0 + r0, u = t1 + r0;
-    round(t, t + LR < t1 ? t + LR : t1, u, u + LR < u1 ? u + LR : u1);
+    const int t = t0 + r0, u = t1 + r0, ue = u + LR < u1 ? u + LR : u1;
+    W w;
+    row.load<LR>(u, ue, w);
+    row.prefix<D, LR>(t, t + LR < t1 ? t + LR : t1, ring, rmask);
+    row.betas<LR>(u, ue, w, ring, rmask, x0v);
     __syncthreads();
+  }
+}
+
+// One warp per (row, k-point), eight rows of a row group per CTA and no
+// block barrier: the warp's G = 32/m lane groups take consecutive runs of
+// a chunk of G LR positions, the ring of a warp holding a chunk and the D
+// positions before it; a chunk's betas and its prefix sums are separated
+// by __syncwarp.  Rows of one group read the same neighbour rows, which the
+// warps of a CTA then share through L1.
+template <typename S, typename R, int D, int LR>
+__global__ void __launch_bounds__(256, 2)
+    k_node_gs_warp(int n, int m, int K, const double* __restrict__ ph, Sc inv_ac_s, Sc third_s, int j0,
+                   int jstep, int nrows, int backward, int rmask, const S* __restrict__ b, S* x) {
+  extern __shared__ float smn[];
+  const int k = blockIdx.y, wid = threadIdx.x >> 5, lane = threadIdx.x & 31, G = 32 / m;
+  const int r = blockIdx.x * 8 + wid;
+  if (r >= nrows || lane >= G * m) return;
+  const int v = lane % m, g = lane / m, CH = G * LR;
+  cx<R>* wbase = reinterpret_cast<cx<R>*>(smn) + (size_t) wid * (rmask + 2) * m;
+  cx<R>* ring = wbase + v;                            // (rmask + 1) * m
+  cx<R>* x0s = wbase + (size_t) (rmask + 1) * m;      // m
+  const GsRow<S, R> row(n, m, K, k, v, j0 + r * jstep, backward, ph, inv_ac_s, third_s, b, x);
+  using W = typename GsRow<S, R>::template Win<LR>;
+  const unsigned mask = G * m == 32 ? 0xffffffffu : (1u << (G * m)) - 1u;
+  if (g == 0) x0s[v] = row.x0();
+  __syncwarp(mask);
+  const cx<R> x0v = x0s[v];
+  for (int c0 = 0; c0 < n; c0 += CH) {
+    const int c1 = c0 + CH < n ? c0 + CH : n;
+    const int u = c0 + g * LR, ue = u + LR < c1 ? u + LR : c1;
+    W w;
+    row.load<LR>(u, ue, w);
+    row.betas<LR>(u, ue, w, ring, rmask, x0v);
+    __syncwarp(mask);
+    row.prefix<D, LR>(u, ue, ring, rmask);
+    __syncwarp(mask);
   }
 }
 
@@ -1091,14 +1165,26 @@ static int L_node_apply(int n, int m, int K, const double* ph, double alpha, dou
 template <typename S, typename R, int D, int LR>
 static int L_node_gs_rows_d(int n, int m, int K, const double* ph, double alpha, int j0, int jstep, int nrows,
                             int backward, const void* b, void* x, cudaStream_t st) {
-  dim3 g(nrows, K), b2 = blk2(m);
+  const Sc inv_ac = make_sc(3.0 / (8.0 * alpha)), third = make_sc(alpha / 3.0);
   int ring = 1;
-  while (ring < 2 * (int) b2.y * LR + D) ring <<= 1;
-  size_t smem = (size_t) (ring + 1) * m * sizeof(cx<R>);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_node_gs_row<S, R, D, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  k_node_gs_row<S, R, D, LR><<<g, b2, smem, st>>>(n, m, K, ph, make_sc(3.0 / (8.0 * alpha)), make_sc(alpha / 3.0),
-                                                   j0, jstep, backward, ring - 1, (const S*) b, (S*) x);
+  if (nrows == 1 || m > 32) {
+    // a single row: a CTA of 256 / m position lanes per k-point
+    dim3 g(nrows, K), b2 = blk2(m);
+    while (ring < 2 * (int) b2.y * LR + D) ring <<= 1;
+    size_t smem = (size_t) (ring + 1) * m * sizeof(cx<R>);
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_node_gs_row<S, R, D, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_node_gs_row<S, R, D, LR><<<g, b2, smem, st>>>(n, m, K, ph, inv_ac, third, j0, jstep, backward, ring - 1,
+                                                     (const S*) b, (S*) x);
+  } else {
+    // a row group: a warp per row
+    while (ring < (32 / m) * LR + D) ring <<= 1;
+    size_t smem = (size_t) 8 * (ring + 1) * m * sizeof(cx<R>);
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_node_gs_warp<S, R, D, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    k_node_gs_warp<S, R, D, LR><<<dim3((nrows + 7) / 8, K), 256, smem, st>>>(
+        n, m, K, ph, inv_ac, third, j0, jstep, nrows, backward, ring - 1, (const S*) b, (S*) x);
+  }
   MX_CHECK_LAUNCH();
   return 0;
 }
