@@ -498,75 +498,131 @@ __global__ void k_block_combine(CombArgs a, SO* __restrict__ out) {
 constexpr int CT = 256;       // threads
 constexpr int CTE = 64;       // entries per tile
 
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// A thread combines a 2x2 tile of outputs: entries ep and ep + 32 of the
+// tile, columns cp and cp + 8, so that each source value and coefficient
+// it loads from shared memory serves two outputs.  The source tiles (CTE
+// entries of each block, contiguous in memory) are copied into shared
+// memory by cp.async, double-buffered: the copies of a CTA's next tile are
+// in flight while it combines the current one.  Every source block and
+// tile starts on a 16-byte boundary (checked at launch).
 template <bool DDOUT>
-__global__ void __launch_bounds__(CT) k_block_combine_tiled(CombArgs a, void* out) {
+__global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void* out) {
   const int k = blockIdx.y, m = a.m, nb = a.nb, nsrc = nb * m;
-  __shared__ float4 cS[48 * 16];            // coefficient pairs [row][column]
-  __shared__ float4 tE[CTE * 16];           // float-float source tile
-  __shared__ float2 tF[2][CTE * 16];        // c64 source tiles (at most two)
+  extern __shared__ float4 smct[];
+  float4* cS = smct;                                             // [48][16] coefficient pairs [row][column]
+  float4* tE = cS + 48 * 16;                                     // [2][CTE * 16] float-float source tiles
+  float2* tF = reinterpret_cast<float2*>(tE + 2 * CTE * 16);     // [2][2][CTE * 16] c64 source tiles
   const int tid = threadIdx.x;
   for (int q = tid; q < nsrc * m; q += CT) {
     int i = q / m, j = q % m;
     cS[i * 16 + j] = a.cpair[(size_t) k * a.ldc * m + (size_t) j * a.ldc + a.row0 + i];
   }
   const bool dd0 = a.precs[0] == MX_CDD;
-  const int j = tid & 15, e0 = tid >> 4;
-  const bool live = j < m;
+  const int cp = tid & 7, ep = tid >> 3;
+  const int c0 = cp, c1 = cp + 8 < m ? cp + 8 : cp;
+  const bool live = c0 < m, two = cp + 8 < m;
   const size_t per_k = (size_t) 2 * a.n * a.n;           // entries per k-point
   const size_t ntiles = (per_k + CTE - 1) / CTE;
-  for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const size_t e_start = tile * CTE;
+  // copies of tile t into buffer q, one commit group per tile
+  auto issue = [&](size_t t, int q) {
+    const size_t e_start = t * CTE;
     const int nte = (int) (per_k - e_start < (size_t) CTE ? per_k - e_start : (size_t) CTE);
-    __syncthreads();
+    const size_t off = ((size_t) k * per_k + e_start) * m;
+    const int len = nte * m;   // elements; even, so that c64 tiles are whole 16-byte units
     for (int b = 0; b < nb; b++) {
-      const size_t off = ((size_t) k * per_k + e_start) * m;
-      const int len = nte * m;
       if (b == 0 && dd0) {
         const float4* src = (const float4*) a.ptrs[0] + off;
-        for (int q = tid; q < len; q += CT) tE[q] = src[q];
+        float4* dst = tE + q * CTE * 16;
+        for (int u = tid; u < len; u += CT) cp_async16(dst + u, src + u);
       } else {
         const float2* src = (const float2*) a.ptrs[b] + off;
-        float2* dst = tF[dd0 ? b - 1 : b];
-        for (int q = tid; q < len; q += CT) dst[q] = src[q];
+        float2* dst = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 16;
+        for (int u = 2 * tid; u < len; u += 2 * CT) cp_async16(dst + u, src + u);
       }
     }
+  };
+  int q = 0;
+  if ((size_t) blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  cp_async_commit();
+  for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, q ^= 1) {
+    if (tile + gridDim.x < ntiles) issue(tile + gridDim.x, q ^ 1);
+    cp_async_commit();
+    cp_async_wait1();
     __syncthreads();
-    if (!live) continue;
-#pragma unroll
-    for (int qq = 0; qq < 4; qq++) {
-      const int e = e0 + 16 * qq;
-      if (e >= nte) break;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};     // compensated sums re (s, c), im (s, c)
-      float fre = 0.f, fim = 0.f;
+    const size_t e_start = tile * CTE;
+    const int nte = (int) (per_k - e_start < (size_t) CTE ? per_k - e_start : (size_t) CTE);
+    // the second entry repeats the first past the tile's end (not written)
+    const int ea = ep, eb = ep + 32 < nte ? ep + 32 : ep;
+    if (live && ea < nte) {
+      // output (entry r, column s) at index 2 r + s, r, s in {0, 1}
+      float acc[4][4] = {};     // compensated sums re (s, c), im (s, c)
+      float fre[4] = {}, fim[4] = {};
       int row = 0;
       if (dd0) {
+        const float4* tEq = tE + q * CTE * 16;
+#pragma unroll 4
         for (int i = 0; i < m; i++) {
-          float4 c = cS[i * 16 + j], v = tE[e * m + i];
-          comp_mac(acc[0], acc[1], c.x, c.y, v.x, v.y);
-          comp_mac(acc[0], acc[1], -c.z, -c.w, v.z, v.w);
-          comp_mac(acc[2], acc[3], c.x, c.y, v.z, v.w);
-          comp_mac(acc[2], acc[3], c.z, c.w, v.x, v.y);
+          const float4 c[2] = {cS[i * 16 + c0], cS[i * 16 + c1]};
+          const float4 v[2] = {tEq[ea * m + i], tEq[eb * m + i]};
+#pragma unroll
+          for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int t = 0; t < 2; t++) {
+              float* ac = acc[2 * r + t];
+              comp_mac(ac[0], ac[1], c[t].x, c[t].y, v[r].x, v[r].y);
+              comp_mac(ac[0], ac[1], -c[t].z, -c[t].w, v[r].z, v[r].w);
+              comp_mac(ac[2], ac[3], c[t].x, c[t].y, v[r].z, v[r].w);
+              comp_mac(ac[2], ac[3], c[t].z, c[t].w, v[r].x, v[r].y);
+            }
         }
         row = m;
       }
       for (int b = dd0 ? 1 : 0; b < nb; b++) {
-        const float2* t = tF[dd0 ? b - 1 : b] + e * m;
-        for (int i = 0; i < m; i++, row++) {
-          float4 c = cS[row * 16 + j];
-          float2 v = t[i];
-          fre = fmaf(c.x, v.x, fmaf(-c.z, v.y, fre));
-          fim = fmaf(c.x, v.y, fmaf(c.z, v.x, fim));
+        const float2* tb = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 16;
+#pragma unroll 4
+        for (int i = 0; i < m; i++) {
+          const float4 c[2] = {cS[(row + i) * 16 + c0], cS[(row + i) * 16 + c1]};
+          const float2 v[2] = {tb[ea * m + i], tb[eb * m + i]};
+#pragma unroll
+          for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int t = 0; t < 2; t++) {
+              fre[2 * r + t] = fmaf(c[t].x, v[r].x, fmaf(-c[t].z, v[r].y, fre[2 * r + t]));
+              fim[2 * r + t] = fmaf(c[t].x, v[r].y, fmaf(c[t].z, v[r].x, fim[2 * r + t]));
+            }
         }
+        row += m;
       }
-      const size_t o = ((size_t) k * per_k + e_start + e) * m + j;
-      if (DDOUT) {
-        dd re = two_sum(acc[0], acc[1] + fre), im = two_sum(acc[2], acc[3] + fim);
-        reinterpret_cast<float4*>(out)[o] = make_float4(re.hi, re.lo, im.hi, im.lo);
-      } else {
-        reinterpret_cast<float2*>(out)[o] = make_float2(acc[0] + acc[1] + fre, acc[2] + acc[3] + fim);
-      }
+#pragma unroll
+      for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+          if ((r && eb == ea) || (t && !two)) continue;
+          const int o2 = 2 * r + t;
+          const size_t o = ((size_t) k * per_k + e_start + (r ? eb : ea)) * m + (t ? c1 : c0);
+          if (DDOUT) {
+            dd re = two_sum(acc[o2][0], acc[o2][1] + fre[o2]), im = two_sum(acc[o2][2], acc[o2][3] + fim[o2]);
+            reinterpret_cast<float4*>(out)[o] = make_float4(re.hi, re.lo, im.hi, im.lo);
+          } else {
+            reinterpret_cast<float2*>(out)[o] =
+                make_float2(acc[o2][0] + acc[o2][1] + fre[o2], acc[o2][2] + acc[o2][3] + fim[o2]);
+          }
+        }
     }
+    // the buffer is refilled by the next iteration's copies
+    __syncthreads();
   }
+}
+
+static size_t combine_tiled_smem() {
+  return sizeof(float4) * (48 * 16 + 2 * CTE * 16) + sizeof(float2) * 4 * CTE * 16;
 }
 
 // ------------------------------------------------------------------
@@ -960,12 +1016,26 @@ extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, 
   for (int q = 1; q < nb; q++) rest64 = rest64 && precs[q] == MX_C64;
   bool first_ok = precs[0] == MX_CDD || precs[0] == MX_C64;
   int nfloat = precs[0] == MX_CDD ? nb - 1 : nb;
-  if (m <= 16 && nfloat <= 2 && first_ok && rest64 && (pout == MX_CDD || (pout == MX_C64 && precs[0] == MX_C64))) {
+  // the tiles' cp.async copies need 16-byte aligned sources and an even
+  // entry count per tile (2 n^2 m entries per k-point: even)
+  bool aligned = true;
+  for (int q = 0; q < nb; q++) aligned = aligned && ((uintptr_t) ptrs[q] & 15) == 0;
+  if (m <= 16 && nfloat <= 2 && first_ok && rest64 && aligned &&
+      (pout == MX_CDD || (pout == MX_C64 && precs[0] == MX_C64))) {
+    // one wave of CTAs, two per SM (152 SMs), each walking tiles of its k-point
     size_t ntiles = (2 * (size_t) n * n + CTE - 1) / CTE;
-    unsigned gx = (unsigned) (ntiles < 64 ? ntiles : 64);
+    size_t want = (size_t) (2 * 152) / (size_t) K;
+    if (want < 1) want = 1;
+    unsigned gx = (unsigned) (ntiles < want ? ntiles : want);
     dim3 g2(gx, K);
-    if (pout == MX_CDD) k_block_combine_tiled<true><<<g2, CT, 0, st>>>(a, out);
-    else k_block_combine_tiled<false><<<g2, CT, 0, st>>>(a, out);
+    size_t sm = combine_tiled_smem();
+    if (pout == MX_CDD) {
+      cudaFuncSetAttribute(k_block_combine_tiled<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+      k_block_combine_tiled<true><<<g2, CT, sm, st>>>(a, out);
+    } else {
+      cudaFuncSetAttribute(k_block_combine_tiled<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+      k_block_combine_tiled<false><<<g2, CT, sm, st>>>(a, out);
+    }
     MX_CHECK_LAUNCH();
     return 0;
   }
