@@ -831,32 +831,39 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+// Bilinear prolongation, one thread per (coarse node, vector): the four
+// fine nodes (2ci + oi, 2cj + oj) from the coarse values at the corners of
+// cell (ci, cj), weight alpha * (1/2 per odd coordinate), in the order
+// c00 (+ c10) (+ c01) (+ c11) for every fine node.
 template <typename S, typename R>
 __global__ void k_node_prolong(int nc, int m, int K, const double* __restrict__ ph, Sc alpha,
                                const S* __restrict__ c, S* __restrict__ f) {
-  int nf = 2 * nc;
-  // block (m, rows): x = vector, y = site; grid.y = k-point
-  int k = blockIdx.y, v = threadIdx.x;
-  int site = blockIdx.x * blockDim.y + threadIdx.y;
-  if (site >= nf * nf) return;
-  int i = site % nf, j = site / nf;
+  const int nf = 2 * nc;
+  // block (m, rows): x = vector, y = coarse node; grid.y = k-point
+  const int k = blockIdx.y, v = threadIdx.x;
+  const int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nc * nc) return;
+  const int ci = site % nc, cj = site / nc;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
   const S* cb = c + Lc.node(k, 0, 0, v);
-  int ci = i >> 1, cj = j >> 1, oi = i & 1, oj = j & 1;
-  cx<R> val;
+  cx<R> c00, c10, c01, c11;
   auto body = [&](const auto& C) {
-    val = C(ci, cj);
-    if (oi) val += C(ci + 1, cj);
-    if (oj) val += C(ci, cj + 1);
-    if (oi && oj) val += C(ci + 1, cj + 1);
+    c00 = C(ci, cj); c10 = C(ci + 1, cj); c01 = C(ci, cj + 1); c11 = C(ci + 1, cj + 1);
   };
   if (ci < nc - 1 && cj < nc - 1) body(NAccI<S, R>{cb, nc, m});
   else body(NAcc<S, R>{cb, nc, m, seam_load<R>(ph, K, k, nc)});
-  // weight alpha * (1/2 per odd coordinate): exact powers of two
-  if (oi) val = scal(rc<R>(0.5f), val);
-  if (oj) val = scal(rc<R>(0.5f), val);
-  S* p = f + Lf.node(k, j, i, v);
-  Store<S, R>::st(p, Store<S, R>::ld(p) + scal(sget<R>(alpha), val));
+  // weights: exact powers of two
+  const R h = rc<R>(0.5f), a = sget<R>(alpha);
+  const cx<R> v00 = c00, v10 = scal(h, c00 + c10), v01 = scal(h, c00 + c01);
+  const cx<R> v11 = scal(h, scal(h, c00 + c10 + c01 + c11));
+  S* p0 = f + Lf.node(k, 2 * cj, 2 * ci, v);
+  S* p1 = f + Lf.node(k, 2 * cj + 1, 2 * ci, v);
+  const cx<R> f00 = Store<S, R>::ld(p0), f10 = Store<S, R>::ld(p0 + m), f01 = Store<S, R>::ld(p1),
+              f11 = Store<S, R>::ld(p1 + m);
+  Store<S, R>::st(p0, f00 + scal(a, v00));
+  Store<S, R>::st(p0 + m, f10 + scal(a, v10));
+  Store<S, R>::st(p1, f01 + scal(a, v01));
+  Store<S, R>::st(p1 + m, f11 + scal(a, v11));
 }
 
 template <typename S, typename R>
@@ -1200,8 +1207,8 @@ static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, i
 template <typename S, typename R>
 static int L_node_prolong(int nc, int m, int K, const double* ph, double alpha, const void* c, void* f,
                           cudaStream_t st) {
-  k_node_prolong<S, R><<<grd2((size_t) 4 * nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
-                                                                             (const S*) c, (S*) f);
+  k_node_prolong<S, R><<<grd2((size_t) nc * nc, m, K), blk2(m), 0, st>>>(nc, m, K, ph, make_sc(alpha),
+                                                                         (const S*) c, (S*) f);
   MX_CHECK_LAUNCH();
   return 0;
 }
