@@ -257,10 +257,10 @@ def run_ours(args):
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # DRAM bytes of one four-colour AFW sweep at 512^2 x 32 k x 16 vectors:
-    # dram__bytes_read.sum + dram__bytes_write.sum of one colour launch at
-    # 4 k-points (530.3 MB, one ncu capture), x 8 for 32 k-points, x 4 launches
-    traffic_per_sweep = 4 * 530.3e6 * (NK / 4)
+    # DRAM bytes of one AFW sweep at 512^2 x 32 k x 16 vectors:
+    # dram__bytes_read.sum + dram__bytes_write.sum of one row-pair launch at
+    # 4 k-points (648.1 MB, one ncu capture), x 8 for 32 k-points, x 2 launches
+    traffic_per_sweep = 2 * 648.1e6 * (NK / 4)
     avg_s = (kms / 1e3) / max(kcount, 1)
     achieved = kbytes / avg_s / 1e9 if kcount else None
     out = {
@@ -278,8 +278,9 @@ def run_ours(args):
         "clocks": clock,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic_per_sweep,
-                     "per": "one AFW sweep (4 colour launches)", "algorithmic_bytes": kbytes,
-                     "kernel": "k_edge_gs_colour (AFW sweep in four colours, finest level)", "peak_source": "measured"},
+                     "per": "one AFW sweep (2 row-pair launches)", "algorithmic_bytes": kbytes,
+                     "kernel": "k_edge_gs_rowpair (AFW sweep in four colours, paired by vertex-row parity, "
+                               "finest level)", "peak_source": "measured"},
         "fp64_gpu": {"value": fp64_value, "unit": "k-points/s", "k_points": n64,
                      "speedup_mixed_vs_fp64": value / fp64_value, "max_rel_eig_diff_vs_mixed": agree},
         "steps_per_k": float(np.mean([st.mean() for st in steps_all])),
