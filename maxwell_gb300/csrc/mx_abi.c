@@ -658,7 +658,7 @@ int sygv_matrix_gpu(matrix_gpu *a, matrix_gpu *b, double *lambda, int *info)
   if(b->rows != N || b->K != K) return MXG_EINVAL;
   if(cudaMalloc((void **) &coef, sizeof(double) * 2 * (size_t) N * N * K)) return MXG_ENOMEM;
   if(cudaMalloc((void **) &theta, sizeof(double) * (size_t) N * K)) { cudaFree(coef); return MXG_ENOMEM; }
-  if(cudaMalloc((void **) &work, sizeof(double) * 10 * (size_t) N * N * K)) {
+  if(cudaMalloc((void **) &work, sizeof(double) * mxk_ritz_work_doubles(N) * K)) {
     cudaFree(coef); cudaFree(theta);
     return MXG_ENOMEM;
   }

@@ -117,7 +117,7 @@ __global__ void k_coarse_apply(int N, int m, const MS* __restrict__ ainv, const 
 // t = sgn(tau)/(|tau| + sqrt(1+tau^2)), c = 1/sqrt(1+t^2), s = t c, and
 // V = [[c, s e], [-s conj(e), c]] on (p,q); A <- V^H A V, Z <- Z V.
 // ------------------------------------------------------------------
-__device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd, int* shi, int max_sweeps,
+__device__ void jacobi_cta(int N, int ld, double* A, double* Zm, double* w, double* shd, int* shi, int max_sweeps,
                            bool init = true) {
   // shd: 4 * (N/2 + 1) doubles of rotation data, plus 32 for reductions
   int Np = N + (N & 1);   // pad to even with a dummy index N
@@ -134,14 +134,19 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
   if (init)
     for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
       int i = (int) (e % N), j = (int) (e / N);
-      AT(Zm, N, i, j) = zmk(i == j ? 1.0 : 0.0, 0.0);
-      if (i < j) AT(A, N, i, j) = zconj(AT(A, N, j, i));   // complete from the lower triangle
-      if (i == j) AT(A, N, i, i).im = 0.0;
+      AT(Zm, ld, i, j) = zmk(i == j ? 1.0 : 0.0, 0.0);
+      if (i < j) AT(A, ld, i, j) = zconj(AT(A, ld, j, i));   // complete from the lower triangle
+      if (i == j) AT(A, ld, i, i).im = 0.0;
     }
   __syncthreads();
   double fro = 0.0;
-  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) fro += zabs2(AT(A, N, e % N, e / N));
+  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) fro += zabs2(AT(A, ld, e % N, e / N));
   fro = sqrt(block_sum(fro, red));
+  // rotation passes: the (rotation s, row or column i) items e = s N + i
+  // are dealt to the threads in strides of blockDim.x, with (s, i) advanced
+  // incrementally (no integer division in the loops)
+  const int bq = (int) blockDim.x / N, br = (int) blockDim.x % N;
+  const int s0 = (int) threadIdx.x / N, i0 = (int) threadIdx.x % N;
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
     // Rutishauser's test: a rotation is skipped when |a_pq| is negligible
     // against sqrt(|a_pp a_qq|) or against the norm of the matrix (a block of
@@ -156,12 +161,12 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
         int p = a < b ? a : b, q = a < b ? b : a;
         double c = 1.0, sv = 0.0, xr = 1.0, xi = 0.0;
         if (q < N) {
-          Z apq = AT(A, N, p, q);
+          Z apq = AT(A, ld, p, q);
           double g = sqrt(zabs2(apq));
-          double scale = sqrt(fabs(AT(A, N, p, p).re * AT(A, N, q, q).re));
+          double scale = sqrt(fabs(AT(A, ld, p, p).re * AT(A, ld, q, q).re));
           if (g > 1e-16 * scale && g > 1e-15 * fro) {
             rotated += 1.0;
-            double app = AT(A, N, p, p).re, aqq = AT(A, N, q, q).re;
+            double app = AT(A, ld, p, p).re, aqq = AT(A, ld, q, q).re;
             double tau = (aqq - app) / (2.0 * g);
             double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
             c = 1.0 / sqrt(1.0 + t * t);
@@ -174,30 +179,31 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
       }
       __syncthreads();
       // columns: A <- A V, Z <- Z V
-      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
-        int s = (int) (e / N), i = (int) (e % N);
+      for (int s = s0, i = i0; s < half;
+           s += bq + (i + br >= N), i = i + br >= N ? i + br - N : i + br) {
         int p = pp[s], q = qq[s];
         if (q >= N || sn[s] == 0.0) continue;
         Z ex = zmk(er[s], ei[s]);
         double c = cs[s], sv = sn[s];
-        Z ap = AT(A, N, i, p), aq = AT(A, N, i, q);
-        AT(A, N, i, p) = zsub(zscal(c, ap), zscal(sv, zmul(zconj(ex), aq)));
-        AT(A, N, i, q) = zadd(zscal(sv, zmul(ex, ap)), zscal(c, aq));
-        Z zp = AT(Zm, N, i, p), zq = AT(Zm, N, i, q);
-        AT(Zm, N, i, p) = zsub(zscal(c, zp), zscal(sv, zmul(zconj(ex), zq)));
-        AT(Zm, N, i, q) = zadd(zscal(sv, zmul(ex, zp)), zscal(c, zq));
+        Z ap = AT(A, ld, i, p), aq = AT(A, ld, i, q);
+        AT(A, ld, i, p) = zsub(zscal(c, ap), zscal(sv, zmul(zconj(ex), aq)));
+        AT(A, ld, i, q) = zadd(zscal(sv, zmul(ex, ap)), zscal(c, aq));
+        Z zp = AT(Zm, ld, i, p), zq = AT(Zm, ld, i, q);
+        AT(Zm, ld, i, p) = zsub(zscal(c, zp), zscal(sv, zmul(zconj(ex), zq)));
+        AT(Zm, ld, i, q) = zadd(zscal(sv, zmul(ex, zp)), zscal(c, zq));
       }
       __syncthreads();
       // rows: A <- V^H A
-      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
-        int s = (int) (e / N), j = (int) (e % N);
+      for (int s = s0, i = i0; s < half;
+           s += bq + (i + br >= N), i = i + br >= N ? i + br - N : i + br) {
+        const int j = i;
         int p = pp[s], q = qq[s];
         if (q >= N || sn[s] == 0.0) continue;
         Z ex = zmk(er[s], ei[s]);
         double c = cs[s], sv = sn[s];
-        Z ap = AT(A, N, p, j), aq = AT(A, N, q, j);
-        AT(A, N, p, j) = zsub(zscal(c, ap), zscal(sv, zmul(ex, aq)));
-        AT(A, N, q, j) = zadd(zscal(sv, zmul(zconj(ex), ap)), zscal(c, aq));
+        Z ap = AT(A, ld, p, j), aq = AT(A, ld, q, j);
+        AT(A, ld, p, j) = zsub(zscal(c, ap), zscal(sv, zmul(ex, aq)));
+        AT(A, ld, q, j) = zadd(zscal(sv, zmul(zconj(ex), ap)), zscal(c, aq));
       }
       __syncthreads();
     }
@@ -206,7 +212,7 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
   // eigenvalues, then sort ascending (selection sort by one thread on the
   // index permutation; N <= 256)
   if (threadIdx.x == 0) {
-    for (int i = 0; i < N; i++) w[i] = AT(A, N, i, i).re;
+    for (int i = 0; i < N; i++) w[i] = AT(A, ld, i, i).re;
     for (int i = 0; i < N; i++) {
       int mi = i;
       for (int j = i + 1; j < N; j++)
@@ -214,9 +220,9 @@ __device__ void jacobi_cta(int N, double* A, double* Zm, double* w, double* shd,
       if (mi != i) {
         double tw = w[i]; w[i] = w[mi]; w[mi] = tw;
         for (int r = 0; r < N; r++) {
-          Z tz = AT(Zm, N, r, i);
-          AT(Zm, N, r, i) = AT(Zm, N, r, mi);
-          AT(Zm, N, r, mi) = tz;
+          Z tz = AT(Zm, ld, r, i);
+          AT(Zm, ld, r, i) = AT(Zm, ld, r, mi);
+          AT(Zm, ld, r, mi) = tz;
         }
       }
     }
@@ -239,7 +245,7 @@ struct Cf {
 };
 
 // one cyclic Jacobi run on the FP32 copy (the same rotation as jacobi_cta)
-__device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* shi, int max_sweeps) {
+__device__ void jacobi_f32(int N, int ld, Cf* A, Cf* Zm, float* shf, double* red, int* shi, int max_sweeps) {
   int Np = N + (N & 1);
   int half = Np / 2;
   float* cs = shf;
@@ -248,13 +254,18 @@ __device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* s
   float* ei = shf + 3 * half;
   int* pp = shi;
   int* qq = shi + half;
-#define AF(M, i, j) (M[(size_t) (j) * N + (i)])
+#define AF(M, i, j) (M[(size_t) (j) * ld + (i)])
   double fro = 0.0;
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
-    Cf a = A[e];
+    Cf a = AF(A, e % N, e / N);
     fro += (double) a.re * a.re + (double) a.im * a.im;
   }
   float frof = (float) sqrt(block_sum(fro, red));
+  // rotation passes: the (rotation s, row or column i) items e = s N + i
+  // are dealt to the threads in strides of blockDim.x, with (s, i) advanced
+  // incrementally (no integer division in the loops)
+  const int bq = (int) blockDim.x / N, br = (int) blockDim.x % N;
+  const int s0 = (int) threadIdx.x / N, i0 = (int) threadIdx.x % N;
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
     double rotated = 0.0;
     for (int r = 0; r < Np - 1; r++) {
@@ -283,8 +294,8 @@ __device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* s
         pp[s] = p; qq[s] = q; cs[s] = c; sn[s] = sv; er[s] = xr; ei[s] = xi;
       }
       __syncthreads();
-      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
-        int s = (int) (e / N), i = (int) (e % N);
+      for (int s = s0, i = i0; s < half;
+           s += bq + (i + br >= N), i = i + br >= N ? i + br - N : i + br) {
         int p = pp[s], q = qq[s];
         if (q >= N || sn[s] == 0.0f) continue;
         float c = cs[s], sv = sn[s], xr = er[s], xi = ei[s];
@@ -297,8 +308,9 @@ __device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* s
         AF(Zm, i, q) = Cf{sv * (xr * zp.re - xi * zp.im) + c * zq.re, sv * (xr * zp.im + xi * zp.re) + c * zq.im};
       }
       __syncthreads();
-      for (size_t e = threadIdx.x; e < (size_t) half * N; e += blockDim.x) {
-        int s = (int) (e / N), j = (int) (e % N);
+      for (int s = s0, i = i0; s < half;
+           s += bq + (i + br >= N), i = i + br >= N ? i + br - N : i + br) {
+        const int j = i;
         int p = pp[s], q = qq[s];
         if (q >= N || sn[s] == 0.0f) continue;
         float c = cs[s], sv = sn[s], xr = er[s], xi = ei[s];
@@ -314,56 +326,60 @@ __device__ void jacobi_f32(int N, Cf* A, Cf* Zm, float* shf, double* red, int* s
 #undef AF
 }
 
-// C = op(X) Y for N x N complex FP64 matrices, op = conjugate transpose when cx
-__device__ void zgemm_cta(int N, double* X, bool cx, double* Y, double* C) {
+// C = op(X) Y for N x N complex FP64 matrices (leading dimension ld), op =
+// conjugate transpose when cx
+__device__ void zgemm_cta(int N, int ld, double* X, bool cx, double* Y, double* C) {
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
     int i = (int) (e % N), j = (int) (e / N);
     Z s = zmk(0.0, 0.0);
     if (cx)
-      for (int l = 0; l < N; l++) s = zadd(s, zcmul(AT(X, N, l, i), AT(Y, N, l, j)));
+      for (int l = 0; l < N; l++) s = zadd(s, zcmul(AT(X, ld, l, i), AT(Y, ld, l, j)));
     else
-      for (int l = 0; l < N; l++) s = zadd(s, zmul(AT(X, N, i, l), AT(Y, N, l, j)));
-    AT(C, N, i, j) = s;
+      for (int l = 0; l < N; l++) s = zadd(s, zmul(AT(X, ld, i, l), AT(Y, ld, l, j)));
+    AT(C, ld, i, j) = s;
   }
   __syncthreads();
 }
 
 // Eigen-decomposition of the Hermitian A (lower triangle used; overwritten)
 // into w (ascending) and Zm.  Buffers: F (N*N complex doubles of space: the
-// FP32 copies, later Q) and G (N*N complex doubles).
-__device__ void jacobi_mixed(int N, double* A, double* Zm, double* w, double* shd, int* shi, double* F, double* G) {
+// FP32 copies, later Q) and G (N*N complex doubles); all with leading
+// dimension ld.
+__device__ void jacobi_mixed(int N, int ld, double* A, double* Zm, double* w, double* shd, int* shi, double* F,
+                             double* G) {
   int half = (N + (N & 1)) / 2;
   double* red = shd + 4 * (half + 1);
   Cf* Af = reinterpret_cast<Cf*>(F);
-  Cf* Zf = Af + (size_t) N * N;
+  Cf* Zf = Af + (size_t) ld * N;
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
     int i = (int) (e % N), j = (int) (e / N);
-    Z a = i >= j ? AT(A, N, i, j) : zconj(AT(A, N, j, i));
+    Z a = i >= j ? AT(A, ld, i, j) : zconj(AT(A, ld, j, i));
     if (i == j) a.im = 0.0;
-    if (i <= j) AT(A, N, i, j) = a;   // complete the FP64 matrix as well
-    Af[e] = Cf{(float) a.re, (float) a.im};
-    Zf[e] = Cf{i == j ? 1.0f : 0.0f, 0.0f};
+    if (i <= j) AT(A, ld, i, j) = a;   // complete the FP64 matrix as well
+    Af[(size_t) j * ld + i] = Cf{(float) a.re, (float) a.im};
+    Zf[(size_t) j * ld + i] = Cf{i == j ? 1.0f : 0.0f, 0.0f};
   }
   __syncthreads();
-  jacobi_f32(N, Af, Zf, reinterpret_cast<float*>(shd), red, shi, 30);
-  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x)
+  jacobi_f32(N, ld, Af, Zf, reinterpret_cast<float*>(shd), red, shi, 30);
+  for (size_t e = threadIdx.x; e < (size_t) ld * N; e += blockDim.x)
     reinterpret_cast<Z*>(Zm)[e] = zmk((double) Zf[e].re, (double) Zf[e].im);
   __syncthreads();
   // Q = Z (3I - Z^H Z) / 2 into F
-  zgemm_cta(N, Zm, true, Zm, G);
+  zgemm_cta(N, ld, Zm, true, Zm, G);
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) {
     int i = (int) (e % N), j = (int) (e / N);
-    Z g = reinterpret_cast<Z*>(G)[e];
-    reinterpret_cast<Z*>(G)[e] = zmk((i == j ? 1.5 : 0.0) - 0.5 * g.re, -0.5 * g.im);
+    Z g = AT(G, ld, i, j);
+    AT(G, ld, i, j) = zmk((i == j ? 1.5 : 0.0) - 0.5 * g.re, -0.5 * g.im);
   }
   __syncthreads();
-  zgemm_cta(N, Zm, false, G, F);
+  zgemm_cta(N, ld, Zm, false, G, F);
   // A' = Q^H A Q, then the FP64 sweeps accumulate onto Q
-  zgemm_cta(N, A, false, F, G);
-  zgemm_cta(N, F, true, G, A);
-  for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x) reinterpret_cast<Z*>(Zm)[e] = reinterpret_cast<Z*>(F)[e];
+  zgemm_cta(N, ld, A, false, F, G);
+  zgemm_cta(N, ld, F, true, G, A);
+  for (size_t e = threadIdx.x; e < (size_t) ld * N; e += blockDim.x)
+    reinterpret_cast<Z*>(Zm)[e] = reinterpret_cast<Z*>(F)[e];
   __syncthreads();
-  jacobi_cta(N, A, Zm, w, shd, shi, 20, false);
+  jacobi_cta(N, ld, A, Zm, w, shd, shi, 20, false);
 }
 
 __global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
@@ -371,11 +387,14 @@ __global__ void k_heev(int N, double* a, double* zwork, double* w, int* info) {
   int half = (N + 1) / 2 + 1;
   double* A = a + (size_t) blockIdx.x * 2 * N * N;
   double* Zm = zwork + (size_t) blockIdx.x * 2 * N * N;
-  jacobi_cta(N, A, Zm, w + (size_t) blockIdx.x * N, sm, reinterpret_cast<int*>(sm + 4 * half + 32), 60);
+  jacobi_cta(N, N, A, Zm, w + (size_t) blockIdx.x * N, sm, reinterpret_cast<int*>(sm + 4 * half + 32), 60);
   for (size_t e = threadIdx.x; e < (size_t) N * N; e += blockDim.x)
     reinterpret_cast<Z*>(A)[e] = reinterpret_cast<Z*>(Zm)[e];
   if (threadIdx.x == 0 && info) info[blockIdx.x] = 0;
 }
+
+// odd leading dimension of the Ritz work matrices
+__host__ __device__ inline int ritz_ld(int ns) { return ns | 1; }
 
 // ------------------------------------------------------------------
 // Rayleigh-Ritz from Gram matrices (see mx_internal.h)
@@ -398,20 +417,24 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   const double* GM = gm + (size_t) k * 2 * ns * ns;
   // work matrices: in shared memory for the Ritz systems (ns <= 48), in
   // global memory for the coarse-grid eigenproblem
+  // every work matrix has the odd leading dimension ld >= ns: a row of a
+  // column-major matrix then falls into distinct shared-memory banks
+  const int ld = ritz_ld(ns);
+  const size_t msz = (size_t) 2 * ld * ns;           // doubles per work matrix
   double* W0;
   if (in_smem) {
     uintptr_t p0 = reinterpret_cast<uintptr_t>(cnt + 2);
     W0 = reinterpret_cast<double*>((p0 + 15) & ~(uintptr_t) 15);
   } else {
-    W0 = work + (size_t) k * 10 * ns * ns;
+    W0 = work + (size_t) k * 5 * msz;
   }
-  double* W1 = W0 + 2 * ns * ns;                     // T = D R^-1
-  double* W2 = W1 + 2 * ns * ns;                     // G_A T, then projected A
-  double* W3 = W2 + 2 * ns * ns;                     // Jacobi eigenvectors
-  double* GS = in_smem ? W3 + 2 * ns * ns : nullptr; // G_A on the selected columns
+  double* W1 = W0 + msz;                             // T = D R^-1
+  double* W2 = W1 + msz;                             // G_A T, then projected A
+  double* W3 = W2 + msz;                             // Jacobi eigenvectors
+  double* GS = in_smem ? W3 + msz : nullptr;         // G_A on the selected columns
   // work of the mixed Jacobi: W0 (free once T is formed) and GS, or in global
   // memory a fifth matrix
-  double* GB = in_smem ? GS : W3 + 2 * ns * ns;
+  double* GB = in_smem ? GS : W3 + msz;
   if (threadIdx.x == 0) {
     int na = 0;
     for (int i = 0; i < ns; i++)
@@ -428,25 +451,25 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   for (size_t e = threadIdx.x; e < (size_t) na * na; e += blockDim.x) {
     int i = (int) (e % na), j = (int) (e / na);
     Z g = reinterpret_cast<const Z*>(GM)[(size_t) idx[j] * ns + idx[i]];
-    AT(W0, na, i, j) = zscal(d[i] * d[j], g);
+    AT(W0, ld, i, j) = zscal(d[i] * d[j], g);
   }
   __syncthreads();
   // right-looking Cholesky with column dropping: W0 -> R (upper), kept flags
   for (int j = 0; j < na; j++) {
-    double piv = AT(W0, na, j, j).re;
+    double piv = AT(W0, ld, j, j).re;
     bool keep = piv > drop && d[j] > 0.0;
     double rjj = keep ? sqrt(piv) : 0.0;
     __syncthreads();
     if (threadIdx.x == 0) kept[j] = keep;
     for (int l = j + threadIdx.x; l < na; l += blockDim.x) {
-      Z v = AT(W0, na, j, l);
-      AT(W0, na, j, l) = keep ? (l == j ? zmk(rjj, 0.0) : zscal(1.0 / rjj, v)) : zmk(0.0, 0.0);
+      Z v = AT(W0, ld, j, l);
+      AT(W0, ld, j, l) = keep ? (l == j ? zmk(rjj, 0.0) : zscal(1.0 / rjj, v)) : zmk(0.0, 0.0);
     }
     __syncthreads();
     if (keep)
       for (size_t e = threadIdx.x; e < (size_t) (na - j - 1) * (na - j - 1); e += blockDim.x) {
         int i = j + 1 + (int) (e % (na - j - 1)), l = j + 1 + (int) (e / (na - j - 1));
-        if (i <= l) AT(W0, na, i, l) = zsub(AT(W0, na, i, l), zcmul(AT(W0, na, j, i), AT(W0, na, j, l)));
+        if (i <= l) AT(W0, ld, i, l) = zsub(AT(W0, ld, i, l), zcmul(AT(W0, ld, j, i), AT(W0, ld, j, l)));
       }
     __syncthreads();
   }
@@ -465,21 +488,21 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   }
   // T (na x r): column c solves R[kept,kept] t = e_c, rows scaled by d
   for (int c = threadIdx.x; c < r; c += blockDim.x) {
-    for (int i = 0; i < na; i++) AT(W1, na, i, c) = zmk(0.0, 0.0);
+    for (int i = 0; i < na; i++) AT(W1, ld, i, c) = zmk(0.0, 0.0);
     for (int a = r - 1; a >= 0; a--) {
       int ia = kept[a];
       Z s = zmk(a == c ? 1.0 : 0.0, 0.0);
-      for (int b = a + 1; b < r; b++) s = zsub(s, zmul(AT(W0, na, ia, kept[b]), AT(W1, na, kept[b], c)));
-      AT(W1, na, ia, c) = zscal(1.0 / AT(W0, na, ia, ia).re, s);
+      for (int b = a + 1; b < r; b++) s = zsub(s, zmul(AT(W0, ld, ia, kept[b]), AT(W1, ld, kept[b], c)));
+      AT(W1, ld, ia, c) = zscal(1.0 / AT(W0, ld, ia, ia).re, s);
     }
-    for (int i = 0; i < na; i++) AT(W1, na, i, c) = zscal(d[i], AT(W1, na, i, c));
+    for (int i = 0; i < na; i++) AT(W1, ld, i, c) = zscal(d[i], AT(W1, ld, i, c));
   }
   __syncthreads();
   // W3 <- G_A T  (na x r), then W2 <- T^H W3 (r x r)
   if (GS) {
     for (size_t e = threadIdx.x; e < (size_t) na * na; e += blockDim.x) {
       int i = (int) (e % na), l = (int) (e / na);
-      AT(GS, na, i, l) = reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]];
+      AT(GS, ld, i, l) = reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]];
     }
     __syncthreads();
   }
@@ -487,21 +510,21 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
     int i = (int) (e % na), c = (int) (e / na);
     Z s = zmk(0.0, 0.0);
     if (GS)
-      for (int l = 0; l < na; l++) s = zadd(s, zmul(AT(GS, na, i, l), AT(W1, na, l, c)));
+      for (int l = 0; l < na; l++) s = zadd(s, zmul(AT(GS, ld, i, l), AT(W1, ld, l, c)));
     else
       for (int l = 0; l < na; l++)
-        s = zadd(s, zmul(reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]], AT(W1, na, l, c)));
-    AT(W3, na, i, c) = s;
+        s = zadd(s, zmul(reinterpret_cast<const Z*>(GA)[(size_t) idx[l] * ns + idx[i]], AT(W1, ld, l, c)));
+    AT(W3, ld, i, c) = s;
   }
   __syncthreads();
   for (size_t e = threadIdx.x; e < (size_t) r * r; e += blockDim.x) {
     int a = (int) (e % r), c = (int) (e / r);
     Z s = zmk(0.0, 0.0);
-    for (int l = 0; l < na; l++) s = zadd(s, zcmul(AT(W1, na, l, a), AT(W3, na, l, c)));
-    AT(W2, r, a, c) = s;
+    for (int l = 0; l < na; l++) s = zadd(s, zcmul(AT(W1, ld, l, a), AT(W3, ld, l, c)));
+    AT(W2, ld, a, c) = s;
   }
   __syncthreads();
-  jacobi_mixed(r, W2, W3, wv, shd, shi, W0, GB);
+  jacobi_mixed(r, ld, W2, W3, wv, shd, shi, W0, GB);
   // Ritz values at or below theta_min are spurious (null-space) modes and
   // are passed over, as exp_bloch2d.c:546-551 does for its coarse start
   if (threadIdx.x == 0) {
@@ -523,7 +546,7 @@ __global__ void k_rayleigh_ritz(int ns, int m, const double* __restrict__ ga, co
   for (size_t e = threadIdx.x; e < (size_t) na * m; e += blockDim.x) {
     int i = (int) (e % na), j = (int) (e / na);
     Z s = zmk(0.0, 0.0);
-    for (int l = 0; l < r; l++) s = zadd(s, zmul(AT(W1, na, i, l), AT(W3, r, l, first + j)));
+    for (int l = 0; l < r; l++) s = zadd(s, zmul(AT(W1, ld, i, l), AT(W3, ld, l, first + j)));
     reinterpret_cast<Z*>(coef)[(size_t) k * ns * m + (size_t) j * ns + idx[i]] = s;
   }
   for (int j = threadIdx.x; j < m; j += blockDim.x) theta[(size_t) k * m + j] = wv[first + j];
@@ -568,13 +591,15 @@ extern "C" int mxk_heev(int N, int K, double* a, double* zwork, double* w, int* 
   return 0;
 }
 
+extern "C" size_t mxk_ritz_work_doubles(int ns) { return (size_t) 10 * ritz_ld(ns) * ns; }
+
 extern "C" int mxk_rayleigh_ritz(int ns, int m, int K, const double* ga, const double* gm, const int* sel,
                                  double drop, double theta_min, double* coef, double* theta, int* info,
                                  double* work, mx_stream s) {
   size_t smem = jacobi_smem(ns) + sizeof(int) * (2 * ns + 4) + sizeof(double) * (2 * ns + 2);
   int in_smem = ns <= 48;
   if (in_smem) {
-    smem += 16 + sizeof(double) * 2 * (size_t) ns * ns * 5;
+    smem += 16 + sizeof(double) * 2 * (size_t) ritz_ld(ns) * ns * 5;
     cudaFuncSetAttribute(k_rayleigh_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
   }
   int threads = in_smem ? DT : 1024;

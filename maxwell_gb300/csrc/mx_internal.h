@@ -115,7 +115,8 @@ int mxk_heev(int N, int K, double *a, double *zwork, double *w, int *info, mx_st
  * (pivot^2 <= drop), Jacobi on the projected A.  Outputs the lowest m Ritz
  * values and the ns x m coefficients (zero rows for dropped columns). */
 /* Ritz values <= theta_min are skipped (spurious null-space modes);
- * work: 10*ns*ns doubles per k */
+ * work: mxk_ritz_work_doubles(ns) doubles per k */
+size_t mxk_ritz_work_doubles(int ns);
 int mxk_rayleigh_ritz(int ns, int m, int K, const double *ga, const double *gm,
                       const int *sel, double drop, double theta_min, double *coef, double *theta,
                       int *info, double *work, mx_stream s);

@@ -214,14 +214,14 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
      || dalloc(&s->P, elen(s, o->L) * es_g) || dalloc(&s->Pn, elen(s, o->L) * es_g)
      || dalloc((void **) &s->ga, sizeof(double) * 2 * ns * ns * K) || dalloc((void **) &s->gm, sizeof(double) * 2 * ns * ns * K)
      || dalloc((void **) &s->coef, sizeof(double) * 2 * ns * m * K) || dalloc((void **) &s->theta, sizeof(double) * m * K)
-     || dalloc((void **) &s->rwork, sizeof(double) * 10 * ns * ns * K)
+     || dalloc((void **) &s->rwork, sizeof(double) * mxk_ritz_work_doubles(ns) * K)
      || dalloc((void **) &s->mu, sizeof(double) * m * K) || dalloc((void **) &s->stats, sizeof(double) * NSTAT * m * K)
      || dalloc((void **) &s->sel, sizeof(int) * ns * K) || dalloc((void **) &s->info, sizeof(int) * K)
      || dalloc((void **) &s->cA, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->cM, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->ccoef, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->ctheta, sizeof(double) * (size_t) N0e * K)
-     || dalloc((void **) &s->cwork, sizeof(double) * 10 * (size_t) N0e * N0e * K)
+     || dalloc((void **) &s->cwork, sizeof(double) * mxk_ritz_work_doubles(N0e) * K)
      || dalloc((void **) &s->cinfo, sizeof(int) * K)
      || dalloc((void **) &s->cacc, sizeof(double) * 4 * K * m)
      || dalloc(&s->combw, (size_t) 16 * ns * m * K))
