@@ -590,23 +590,35 @@ __device__ __forceinline__ cx<R> lap_off(const A& V, int i, int j) {
          + V(i - 1, j + 1) + V(i + 1, j + 1);
 }
 
+// y = cy yin + alpha L x, a thread per two neighbouring nodes (i, i+1) of a
+// row and vector, which share six of their nine stencil values
 template <typename S, typename R>
 __global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph, Sc diag, Sc off, Sc cy,
                              int has_cy, const S* __restrict__ x, const S* yin, S* y) {
-  // block (m, rows): x = vector, y = site; grid.y = k-point
-  int k = blockIdx.y, v = threadIdx.x;
-  int site = blockIdx.x * blockDim.y + threadIdx.y;
-  if (site >= n * n) return;
-  int i = site % n, j = site / n;
+  // block (m, rows): x = vector, y = node pair; grid.y = k-point
+  const int k = blockIdx.y, v = threadIdx.x, hp = (n + 1) / 2;
+  const int pair = blockIdx.x * blockDim.y + threadIdx.y;
+  if (pair >= hp * n) return;
+  const int i = 2 * (pair % hp), j = pair / hp;
+  const bool two = i + 1 < n;
   Lay L{n, m, K};
   const S* xb = x + L.node(k, 0, 0, v);
-  cx<R> o;
-  auto body = [&](const auto& V) { o = scal(sget<R>(diag), V(i, j)) + scal(sget<R>(off), lap_off<R>(V, i, j)); };
-  if (i > 0 && i < n - 1 && j > 0 && j < n - 1) body(NAccI<S, R>{xb, n, m});
+  const R dg = sget<R>(diag), of = sget<R>(off);
+  cx<R> o0, o1 = czero<R>();
+  auto body = [&](const auto& V) {
+    o0 = scal(dg, V(i, j)) + scal(of, lap_off<R>(V, i, j));
+    if (two) o1 = scal(dg, V(i + 1, j)) + scal(of, lap_off<R>(V, i + 1, j));
+  };
+  if (i > 0 && i + 2 < n && j > 0 && j < n - 1) body(NAccI<S, R>{xb, n, m});
   else body(NAcc<S, R>{xb, n, m, seam_load<R>(ph, K, k, n)});
-  size_t at = L.node(k, j, i, v);
-  if (has_cy) o += scal(sget<R>(cy), Store<S, R>::ld((yin ? yin : y) + at));
-  Store<S, R>::st(y + at, o);
+  const size_t at = L.node(k, j, i, v);
+  const S* yr = yin ? yin : y;
+  if (has_cy) {
+    o0 += scal(sget<R>(cy), Store<S, R>::ld(yr + at));
+    if (two) o1 += scal(sget<R>(cy), Store<S, R>::ld(yr + at + m));
+  }
+  Store<S, R>::st(y + at, o0);
+  if (two) Store<S, R>::st(y + at + m, o1);
 }
 
 template <typename S, typename R>
@@ -1163,7 +1175,7 @@ static int L_edge_restrict(int nc, int m, int K, const double* ph, double alpha,
 template <typename S, typename R>
 static int L_node_apply(int n, int m, int K, const double* ph, double alpha, double cy, const void* x,
                         const void* yin, void* y, cudaStream_t st) {
-  k_node_apply<S, R><<<grd2((size_t) n * n, m, K), blk2(m), 0, st>>>(
+  k_node_apply<S, R><<<grd2((size_t) ((n + 1) / 2) * n, m, K), blk2(m), 0, st>>>(
       n, m, K, ph, make_sc(alpha * 8.0 / 3.0), make_sc(-alpha / 3.0), make_sc(cy), cy != 0.0, (const S*) x,
       (const S*) yin, (S*) y);
   MX_CHECK_LAUNCH();

@@ -80,13 +80,14 @@ def test_afw_smoother(oracle, setup, prec, direction):
 
 
 @pytest.mark.parametrize("n, m, prec", [(16, 4, mx.C64), (80, 4, mx.C64), (256, 16, mx.C64), (128, 16, mx.C128),
-                                         (128, 16, mx.CDD)])
+                                         (128, 16, mx.CDD), (32, 1, mx.C64), (48, 7, mx.C64), (24, 7, mx.C128)])
 @pytest.mark.parametrize("direction", [0, 1, 2])
 def test_node_gs_even_block(oracle, n, m, prec, direction):
     """Node Gauss-Seidel against the oracle: a row in one segment (n = 16,
     80 at 4 vectors) and in several with a partial last one (n = 256 at 16
     c64 vectors: segments of 112 positions; n = 128 at 16 FP64 or
-    float-float vectors: segments of 48)."""
+    float-float vectors: segments of 48); one vector and 7 vectors (lane
+    groups that leave part of a warp idle)."""
     rng = np.random.default_rng(5)
     K = 3
     g = mx.Grid(n, K, None, FACTORS)
@@ -112,6 +113,24 @@ def test_colour_smoother(oracle, setup, prec, direction):
     want = np.array([[oracle.gs_edge_colour(n, kap, *FACTORS[k], 1.0, 1.0, direction, b[k, v], x[k, v])
                       for v in range(m)] for k in range(K)])
     assert rel(ex.get(), want) < (1e-11 if prec != mx.C64 else 1e-4)
+
+
+@pytest.mark.parametrize("n, m", [(16, 1), (24, 7)])
+@pytest.mark.parametrize("prec", [mx.C128, mx.C64])
+@pytest.mark.parametrize("direction", [0, 1])
+def test_colour_smoother_block_sizes(oracle, n, m, prec, direction):
+    """The colour smoother with one vector and with 7 (patch lanes per CTA
+    256 / m), against the oracle's restatement of the same order."""
+    rng = np.random.default_rng(17)
+    K = 2
+    kap = 1.0 / (1.0 + 11.0 * rng.random(n * n))
+    g = mx.Grid(n, K, kap, FACTORS[:K])
+    b, x = cv(rng, K, m, 2 * n * n), cv(rng, K, m, 2 * n * n)
+    eb, ex = mx.Edge(g, m, prec, b), mx.Edge(g, m, prec, x)
+    mx.check(mx.lib().gscolour_edge2d_gpu(mx.fz(1.0), mx.fz(1.0), eb.h, ex.h, direction))
+    want = np.array([[oracle.gs_edge_colour(n, kap, *FACTORS[k], 1.0, 1.0, direction, b[k, v], x[k, v])
+                      for v in range(m)] for k in range(K)])
+    assert rel(ex.get(), want) < (1e-11 if prec == mx.C128 else 1e-4)
 
 
 @pytest.mark.parametrize("smoother", [0, 1])
