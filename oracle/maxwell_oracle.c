@@ -139,28 +139,54 @@ om_addeval_edge(int n, const double *kappa, cx xf, cx yf,
     }
 }
 
+/* Dot products and norms sum fixed chunks of OM_CHUNK entries and combine
+ * the chunk sums in chunk order, so that the result does not depend on the
+ * thread count or on the order in which threads finish. */
+#define OM_CHUNK 4096L
+
 cx
 om_dot(long len, const cx *x, const cx *y)
 {
+  long nc = (len + OM_CHUNK - 1) / OM_CHUNK, c;
+  double *part = malloc(sizeof(double) * 2 * (size_t) (nc > 0 ? nc : 1));
   double re = 0.0, im = 0.0;
-  long k;
-#pragma omp parallel for reduction(+:re,im) schedule(static)
-  for(k = 0; k < len; k++) {
-    cx p = conj(x[k]) * y[k];
-    re += creal(p);
-    im += cimag(p);
+#pragma omp parallel for schedule(static)
+  for(c = 0; c < nc; c++) {
+    long k, k1 = (c + 1) * OM_CHUNK < len ? (c + 1) * OM_CHUNK : len;
+    double r = 0.0, q = 0.0;
+    for(k = c * OM_CHUNK; k < k1; k++) {
+      cx p = conj(x[k]) * y[k];
+      r += creal(p);
+      q += cimag(p);
+    }
+    part[2 * c] = r;
+    part[2 * c + 1] = q;
   }
+  for(c = 0; c < nc; c++) {
+    re += part[2 * c];
+    im += part[2 * c + 1];
+  }
+  free(part);
   return re + I * im;
 }
 
 double
 om_norm2(long len, const cx *x)
 {
+  long nc = (len + OM_CHUNK - 1) / OM_CHUNK, c;
+  double *part = malloc(sizeof(double) * (size_t) (nc > 0 ? nc : 1));
   double s = 0.0;
-  long k;
-#pragma omp parallel for reduction(+:s) schedule(static)
-  for(k = 0; k < len; k++)
-    s += creal(x[k]) * creal(x[k]) + cimag(x[k]) * cimag(x[k]);
+#pragma omp parallel for schedule(static)
+  for(c = 0; c < nc; c++) {
+    long k, k1 = (c + 1) * OM_CHUNK < len ? (c + 1) * OM_CHUNK : len;
+    double r = 0.0;
+    for(k = c * OM_CHUNK; k < k1; k++)
+      r += creal(x[k]) * creal(x[k]) + cimag(x[k]) * cimag(x[k]);
+    part[c] = r;
+  }
+  for(c = 0; c < nc; c++)
+    s += part[c];
+  free(part);
   return sqrt(s);
 }
 
