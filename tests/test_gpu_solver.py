@@ -76,3 +76,21 @@ def test_surface_matches_oracle(oracle):
     assert st_o == 0
     got = lam.reshape(steps * steps, m)[:, :ie]
     assert np.abs(got - lam_o[:, :ie]).max() / lam_o[:, :ie].max() < 1e-8
+
+
+def test_solver_matches_reference_driver_curve(oracle, golden):
+    """The mixed LOBPCG solver on the points of the reference driver's own
+    run (exp_bloch2d: Kivshar disc, 16^2, 4 steps per edge of its curve,
+    absolute residual 1e-8): eigenvalues agree with the driver's protocol to
+    its 6 decimals.  At Gamma the driver keeps the two harmonic zero modes,
+    which the solver's constant-field removal takes out."""
+    g = golden("bloch_curve_n16_kivshar.npz")
+    n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
+    kap = oracle.disc_kappa(n0 << L, [g["disc"]], float(g["eps_base"]))
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, wave=len(g["factors"]), relative=0,
+                  tol=float(g["tol"]), max_nested=40, max_steps=80)
+    lam, steps, res = s.solve(g["factors"])
+    assert res[:, :ie].max() <= float(g["tol"])
+    for k, row in enumerate(g["lam"]):
+        ref = row[:ie][np.abs(row[:ie]) > 1e-3]
+        assert np.abs(lam[k, :len(ref)] - ref).max() < 2e-6, (k, lam[k, :len(ref)], ref)

@@ -196,3 +196,28 @@ def test_oracle_colour_smoother_converges(oracle, golden):
         cur = energy(x - xs)
         assert cur < 0.9 * last
         last = cur
+
+
+def driver_curve_reference(g):
+    """Per point of the reference driver's curve, the converged eigenvalues
+    of its protocol (the first ieigs) without Gamma's two harmonic zero
+    modes, which the driver keeps and the constant-field removal here takes
+    out."""
+    ie = int(g["ieigs"])
+    return [row[:ie][np.abs(row[:ie]) > 1e-3] for row in g["lam"]]
+
+
+def test_oracle_matches_reference_driver_curve(oracle, golden):
+    """The reference's own driver program (exp_bloch2d: Kivshar disc, 16^2,
+    4 steps per edge of its Gamma-X-M-Gamma curve, block PINVIT to the
+    absolute residual 1e-8): the oracle's eigenvalues at the same points
+    agree with its protocol file to the file's 6 decimals."""
+    g = golden("bloch_curve_n16_kivshar.npz")
+    n0, L = int(g["n0"]), int(g["L"])
+    kap = oracle.disc_kappa(n0 << L, [g["disc"]], float(g["eps_base"]))
+    st, lam, steps, res, _ = oracle.bloch_solve(
+        kap, g["factors"], n0=n0, L=L, ieigs=int(g["ieigs"]), m=int(g["m"]), method=0, max_nested=40,
+        max_steps=80, tol=float(g["tol"]), relative=0, extrapolation="2", wave=1)
+    assert st == 0
+    for k, ref in enumerate(driver_curve_reference(g)):
+        assert np.abs(lam[k, :len(ref)] - ref).max() < 2e-6, (k, lam[k, :len(ref)], ref)
