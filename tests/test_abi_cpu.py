@@ -57,3 +57,27 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(mx, "LIB_PATH", str(tmp_path / "absent.so"))
     with pytest.raises(ImportError):
         mx.lib()
+
+
+@pytest.mark.parametrize("cc, lang, std", [("gcc", "c", "c99"), ("gcc", "c", "c11"), ("g++", "c++", "c++17")])
+def test_header_compiles_for_c_and_cpp_callers(cc, lang, std):
+    """The boundary header is plain C that a reference caller (C99, OpenMP)
+    or a C++ host includes without warnings."""
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = '#include "maxwell_gb300.h"\nint main(void) { return 0; }\n'
+    r = subprocess.run([cc, "-x", lang, f"-std={std}", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only",
+                        "-I", inc, "-"], input=src, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_c_caller_links_every_declared_function(built):
+    """A C program that takes the address of every declared function links
+    against the library: declarations and exports agree in name and
+    linkage (nothing runs)."""
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    names = mx.header_functions()
+    body = "\n".join(f"  (void) &{n};" for n in names)
+    src = f'#include "maxwell_gb300.h"\nint main(void) {{\n{body}\n  return 0;\n}}\n'
+    r = subprocess.run(["gcc", "-x", "c", "-std=c11", "-I", inc, "-", "-o", os.devnull, "-L", os.path.dirname(built),
+                        "-l:" + os.path.basename(built)], input=src, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
