@@ -792,17 +792,17 @@ __global__ void __launch_bounds__(256, 2)
   {
     const int u1 = SEG < n ? SEG : n, ue = r0 + LR < u1 ? r0 + LR : u1;
     W w;
-    row.load<LR>(r0, ue, w);
-    row.betas<LR>(r0, ue, w, ring, rmask, x0v);
+    row.template load<LR>(r0, ue, w);
+    row.template betas<LR>(r0, ue, w, ring, rmask, x0v);
   }
   __syncthreads();
   for (int t0 = 0; t0 < n; t0 += SEG) {
     const int t1 = t0 + SEG < n ? t0 + SEG : n, u1 = t1 + SEG < n ? t1 + SEG : n;
     const int t = t0 + r0, u = t1 + r0, ue = u + LR < u1 ? u + LR : u1;
     W w;
-    row.load<LR>(u, ue, w);
-    row.prefix<D, LR>(t, t + LR < t1 ? t + LR : t1, ring, rmask);
-    row.betas<LR>(u, ue, w, ring, rmask, x0v);
+    row.template load<LR>(u, ue, w);
+    row.template prefix<D, LR>(t, t + LR < t1 ? t + LR : t1, ring, rmask);
+    row.template betas<LR>(u, ue, w, ring, rmask, x0v);
     __syncthreads();
   }
 }
@@ -835,10 +835,10 @@ __global__ void __launch_bounds__(256, 2)
     const int c1 = c0 + CH < n ? c0 + CH : n;
     const int u = c0 + g * LR, ue = u + LR < c1 ? u + LR : c1;
     W w;
-    row.load<LR>(u, ue, w);
-    row.betas<LR>(u, ue, w, ring, rmask, x0v);
+    row.template load<LR>(u, ue, w);
+    row.template betas<LR>(u, ue, w, ring, rmask, x0v);
     __syncwarp(mask);
-    row.prefix<D, LR>(u, ue, ring, rmask);
+    row.template prefix<D, LR>(u, ue, ring, rmask);
     __syncwarp(mask);
   }
 }
