@@ -81,3 +81,15 @@ def test_c_caller_links_every_declared_function(built):
     r = subprocess.run(["gcc", "-x", "c", "-std=c11", "-I", inc, "-", "-o", os.devnull, "-L", os.path.dirname(built),
                         "-l:" + os.path.basename(built)], input=src, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_example_compiles():
+    """The C caller shown in INTEGRATION.md compiles against the header
+    without warnings."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    text = open(os.path.join(root, "INTEGRATION.md")).read()
+    start = text.index("```c\n") + len("```c\n")
+    src = text[start:text.index("```", start)]
+    r = subprocess.run(["gcc", "-x", "c", "-std=c11", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(root, "include"), "-"], input=src, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
