@@ -69,6 +69,24 @@ int setkappa_grid2d_gpu(grid2d_gpu *gr, const double *kappa);
 /* gr->xfactor / gr->yfactor for each of the K Bloch parameters */
 int setbloch_grid2d_gpu(grid2d_gpu *gr, const mxg_field *xfactor, const mxg_field *yfactor);
 int getsize_grid2d_gpu(const grid2d_gpu *gr, int *nx, int *K);
+/* the reciprocal permittivity per cell as set on the grid, n*n host doubles */
+int getkappa_grid2d_gpu(const grid2d_gpu *gr, double *kappa);
+/* epspattern (grid2d.h:40-62): rectangles as (eps, left, bottom, width,
+ * height), circles as (eps, centre x, centre y, radius), eps_base around them */
+typedef struct {
+  double *rectangle;
+  int rectangles;
+  double *circle;
+  int circles;
+  double eps_base;
+} mxg_epspattern;
+/* new_epspattern / del_epspattern (grid2d.c:148-169): zeroed shape arrays */
+mxg_epspattern *new_epspattern_gpu(double eps_base, int rectangles, int circles);
+void del_epspattern_gpu(mxg_epspattern *pat);
+/* setpattern_grid2d (grid2d.c:171-218): 1/eps of every cell from the pattern,
+ * each cell tested at its lower-left corner, circles after rectangles; the
+ * rasterisation runs on the device.  A NULL pattern leaves the grid as it is. */
+int setpattern_grid2d_gpu(const mxg_epspattern *pat, grid2d_gpu *gr);
 
 /* ---------- edge2d (edge2d.h:71-291) ---------- */
 edge2d_gpu *new_edge2d_gpu(const grid2d_gpu *gr, int m, int prec);
@@ -77,8 +95,31 @@ size_t getdimension_edge2d_gpu(const edge2d_gpu *x);          /* 2 nx ny per vec
 int zero_edge2d_gpu(edge2d_gpu *x);
 int copy_edge2d_gpu(const edge2d_gpu *x, edge2d_gpu *y);      /* converts precision */
 int add_edge2d_gpu(mxg_field alpha, const edge2d_gpu *x, edge2d_gpu *y);
+/* swap_edge2d (edge2d.c:126-159): exchanges the contents of two batches of
+ * the same shape and precision (their device storage changes hands) */
+int swap_edge2d_gpu(edge2d_gpu *x, edge2d_gpu *y);
+/* random_edge2d (edge2d.c:161-191): real and imaginary parts uniform in
+ * [-1, 1).  The reference draws from rand(); here a counter-based generator
+ * (SplitMix64) keyed by seed gives the same values on every device and
+ * for every launch shape. */
+int random_edge2d_gpu(edge2d_gpu *x, unsigned long long seed);
+/* scale_edge2d (edge2d.c:806-828): x *= alpha */
+int scale_edge2d_gpu(mxg_field alpha, edge2d_gpu *x);
 /* norms and products per (k, vector): out has K*m entries */
 int norm2_edge2d_gpu(const edge2d_gpu *x, double *out);
+/* normmax_edge2d (edge2d.c:887-920): max |x_e| per (k, vector) */
+int normmax_edge2d_gpu(const edge2d_gpu *x, double *out);
+/* dotprod_edge2d (edge2d.c:1207-1238): sum conj(x_e) y_e per (k, vector) */
+int dotprod_edge2d_gpu(const edge2d_gpu *x, const edge2d_gpu *y, mxg_field *out);
+/* nullprod_edge2d (edge2d.c:1240-1274): L2 products of x with the two
+ * constant fields, hy * (sum of the x-edge coefficients) and
+ * hx * (sum of the y-edge coefficients), per (k, vector); xprod or yprod may
+ * be NULL.  Defined for k = 0 (the reference asserts xfactor = yfactor = 1);
+ * computed for every k-point of the batch as given. */
+int nullprod_edge2d_gpu(const edge2d_gpu *x, mxg_field *xprod, mxg_field *yprod);
+/* nulladd_edge2d (edge2d.c:1276-1307): x-edges += hx xalpha, y-edges +=
+ * hy yalpha, one pair of scalars per (k, vector) */
+int nulladd_edge2d_gpu(const mxg_field *xalpha, const mxg_field *yalpha, edge2d_gpu *x);
 int center_edge2d_gpu(edge2d_gpu *x);
 /* No counterpart in the reference.  center_edge2d_gpu for callers that must
  * not allocate device memory (an application that owns a fixed device budget
@@ -90,7 +131,9 @@ int center_edge2d_gpu(edge2d_gpu *x);
  * allocates nothing: its scratch (4 doubles per k-point and vector) is a
  * static device array for at most MXG_CENTER_NOALLOC_MAX_KM (k-point, vector)
  * pairs (256 KiB, held by every GPU that loads the library until exit); a
- * larger K*m returns MXG_EINVAL.  The first call on a device looks up the
+ * larger K*m returns MXG_EINVAL.  The device current for the calling thread
+ * must be the one that owns x, gamma_flag and the stream (a stream of another
+ * device returns MXG_EINVAL).  The first call on a device looks up the
  * array's address there, so make it before any stream capture.  All calls on
  * a device share the array: calls that overlap on the GPU race. */
 #define MXG_CENTER_NOALLOC_MAX_KM 8192
@@ -124,6 +167,24 @@ int densematrix_edge2d_gpu(mxg_field alpha, mxg_field beta, const grid2d_gpu *gr
 /* host <-> device in the reference's dense order (denseto/densefrom_edge2d) */
 int denseto_edge2d_gpu(const mxg_field *host, edge2d_gpu *y);
 int densefrom_edge2d_gpu(const edge2d_gpu *x, mxg_field *host);
+/* The Ritz products of exp_bloch2d.c:991-996 for the whole block in one call:
+ * a[k] = X^H (A+M) X (energyprod_edge2d(1, 1, .)) and m[k] = X^H M X
+ * (massprod_edge2d) for the m vectors of every k-point, full Hermitian
+ * m x m matrices, column-major, K of each; a or m may be NULL; m <= 48 */
+int gram_edge2d_gpu(const edge2d_gpu *x, mxg_field *a, mxg_field *m);
+/* The Ritz combination of exp_bloch2d.c:1006-1010 (e_j = sum_i C_ij u_i,
+ * m^2 add_edge2d calls) in one call: y[k][j] = sum_i coef[k](i, j) x[k][i],
+ * coef K column-major m x m matrices; x and y distinct, same shape */
+int lincomb_edge2d_gpu(const mxg_field *coef, const edge2d_gpu *x, edge2d_gpu *y);
+/* orthonormalize_edge2d (edge2d.c:6264-6296): makes the m vectors of every
+ * k-point orthonormal in the mass inner product, the first j of them
+ * spanning what the first j spanned before.  The reference uses Householder
+ * reflections in the M inner product; this is Cholesky-QR: X^H M X = R^H R,
+ * X <- X R^-1 (R with a positive real diagonal).  info[k] = 0, or j+1 if
+ * column j of k-point k is dependent on the columns before it (the part of
+ * it outside their span has less than 1e-5 of its M-norm); then nothing is
+ * changed and the call returns MXG_ECONV. */
+int orthonormalize_edge2d_gpu(edge2d_gpu *x, int *info);
 
 /* ---------- node2d (node2d.h:28-158) ---------- */
 node2d_gpu *new_node2d_gpu(const grid2d_gpu *gr, int m, int prec);
@@ -142,6 +203,16 @@ int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2
 int densematrix_node2d_gpu(int fixnull, const grid2d_gpu *gr, matrix_gpu *a);
 int denseto_node2d_gpu(const mxg_field *host, node2d_gpu *y);
 int densefrom_node2d_gpu(const node2d_gpu *x, mxg_field *host);
+/* the vector operations of node2d.h:42-84, as their edge counterparts */
+int copy_node2d_gpu(const node2d_gpu *x, node2d_gpu *y);                  /* node2d.c:53-70 */
+int random_node2d_gpu(node2d_gpu *x, unsigned long long seed);            /* node2d.c:72-90 */
+int scale_node2d_gpu(mxg_field alpha, node2d_gpu *x);                     /* node2d.c:385-399 */
+int add_node2d_gpu(mxg_field alpha, const node2d_gpu *x, node2d_gpu *y);  /* node2d.c:401-418 */
+int norm2_node2d_gpu(const node2d_gpu *x, double *out);                   /* node2d.c:420-439 */
+int normmax_node2d_gpu(const node2d_gpu *x, double *out);                 /* node2d.c:441-463 */
+int dotprod_node2d_gpu(const node2d_gpu *x, const node2d_gpu *y, mxg_field *out); /* node2d.c:465-487 */
+/* center_node2d (node2d.c:489-514): subtract the mean coefficient */
+int center_node2d_gpu(node2d_gpu *x);
 
 /* ---------- linalg (linalg.h:7-31): one square matrix per k ---------- */
 matrix_gpu *new_matrix_gpu(int rows, int K);
@@ -152,11 +223,24 @@ int download_matrix_gpu(const matrix_gpu *a, mxg_field *host);
  * as the explicit inverse, so potrsv applies one matrix-vector product;
  * info[k] as zpotrf's */
 int potrf_matrix_gpu(matrix_gpu *a, int *info);
+/* potrsv_matrix (linalg.c:98-113): b <- A^-1 b for every k after
+ * potrf_matrix_gpu; b holds K host vectors of `rows` entries */
+int potrsv_matrix_gpu(const matrix_gpu *a, mxg_field *b);
 /* sygv_matrix (linalg.c:285-317), itype 1: a <- B-orthonormal eigenvectors,
  * lambda (K*rows) ascending, info per k */
 int sygv_matrix_gpu(matrix_gpu *a, matrix_gpu *b, double *lambda, int *info);
 /* syev_matrix (linalg.c:254-283) */
 int syev_matrix_gpu(matrix_gpu *a, double *lambda, int *info);
+
+/* ---------- one PINVIT step (edge2d.h:287-291) ---------- */
+/* pinvit_edge2d (edge2d.c:6298-6328) on level l for every (k, vector) of e:
+ * defect (A+M) e - lambda M e, prec_steps edge V-cycles with smoother_steps
+ * sweeps, e -= update, then the gradient lifting with gradient_steps node
+ * V-cycles.  lambda: K*m host doubles (one shift per vector, as the
+ * reference is called once per vector with its own Rayleigh quotient). */
+int pinvit_edge2d_gpu(int l, int smoother_steps, int prec_steps, int gradient_steps, const double *lambda,
+                      edge2d_gpu *e, const matrix_gpu *Ae, edge2d_gpu **b, edge2d_gpu **x, edge2d_gpu **d,
+                      const matrix_gpu *An, node2d_gpu **bg, node2d_gpu **xg, node2d_gpu **dg);
 
 /* ---------- the per-k eigensolver (exp_bloch2d.c:556-1053) ---------- */
 typedef struct {
@@ -175,32 +259,56 @@ typedef struct {
   int relative;          /* stopping rule: 0 absolute defect, 1 relative residual */
   double tol;
   int smoother;          /* edge smoother: 0 the reference's row order, 1 four colours */
+  double drop;           /* Ritz step: columns whose Cholesky-QR pivot^2 falls below this
+                          * are dropped; 0 = 1e-6 (mixed) or 1e-12 (plain FP64) */
+  int extrapolation;     /* start of every wave after the first, from the same slots of
+                          * earlier waves (exp_bloch2d.c:814-895, maxwell_extra):
+                          * 'n' or 0 their eigenvectors, '1' Rayleigh-Ritz over the last
+                          * two waves, '2' over the last three */
 } mxg_solve_opts;
 
 typedef struct mxg_solver mxg_solver;
+/* Makes CUDA device `device` current for the calling thread (cudaSetDevice):
+ * one process per GPU selects its GPU with this before creating objects.
+ * A solver lives on the device that was current when it was created and
+ * makes that device current again in each of its calls. */
+int mxg_set_device(int device);
 /* kappa_fine: n*n host doubles */
 mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine);
 void mxg_solver_free(mxg_solver *s);
 /* Solve nk k-points (factors e^{i kx}, e^{i ky}); outputs lambda = mu - 1
- * (nk*m), block steps per k (nk), final residual per vector (nk*m) */
+ * (nk*m), block steps per k (nk), final residual per vector (nk*m).  A
+ * k-point within 1e-8 of Gamma (|xf - 1| + |yf - 1| in the 1-norm of the
+ * components) gets the constant-field removal when o.center is set. */
 int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xfactor, const mxg_field *yfactor,
                     double *lambda, int *steps, double *residual);
 /* The full-zone surface of exp_blochsurf (exp_blochsurf.c:25-37, 964-1489):
  * steps x steps k-points k = 2 pi (ix, iy) / (steps - 1) - (pi, pi), solved
  * in waves of o.wave k-points in row order (iy outer); every wave after the
- * first starts from the previous wave's eigenvectors.  Outputs as
- * mxg_bloch_solve, indexed (iy * steps + ix). */
+ * first starts from the earlier waves as o.extrapolation says (with o.wave
+ * = steps, each k-point from the same column of the rows below it, the
+ * reference's extrapolation along y).  Outputs as mxg_bloch_solve, indexed
+ * (iy * steps + ix). */
 int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, double *residual);
 /* eigenvectors of the last solved batch: wave k-points x m vectors in dense order */
 int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of
  * kernel launches it issued */
 int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches);
-/* CUDA-event timing of the finest-level AFW Gauss-Seidel sweeps: total
- * milliseconds and number of sweeps since profiling was enabled, and the
- * algorithmic bytes of one sweep (x, b, kappa read once, x written once) */
+/* warm-started waves of the last mxg_bloch_solve / mxg_bloch_surface that
+ * missed the tolerance and were solved again from a cold start */
+int mxg_solver_restarts(const mxg_solver *s);
+/* CUDA-event timing, on the solver's stream, of three launch sequences at
+ * the finest level: node Gauss-Seidel sweeps of the gradient lifting
+ * (MXG_KT_NODE_GS), AFW sweeps of the preconditioner (MXG_KT_AFW) and the
+ * Gram matrices of the Ritz step (MXG_KT_GRAM).  With profiling enabled the
+ * solver launches the V-cycles directly (no CUDA graph) so that every sweep
+ * carries its own events.  kernel_time returns, since profiling was enabled,
+ * the summed milliseconds, the number of timed sequences and their summed
+ * algorithmic bytes (each array the sequence reads or writes counted once). */
+enum { MXG_KT_NODE_GS = 0, MXG_KT_AFW = 1, MXG_KT_GRAM = 2, MXG_KT_N = 3 };
 int mxg_solver_profile(mxg_solver *s, int enable);
-int mxg_solver_kernel_time(mxg_solver *s, double *ms, long *count, double *bytes_per_sweep);
+int mxg_solver_kernel_time(mxg_solver *s, int which, double *ms, long *count, double *bytes);
 
 /* ---------- eigenvalue sensitivity (no counterpart in the reference) ---------- */
 /* grad[c] = sum_{k,v} w[k*m+v] d lambda_{k,v} / d eps_c for M-normalised

@@ -36,7 +36,15 @@ class SolveOpts(C.Structure):
     _fields_ = [(n, C.c_int) for n in (
         "n0", "L", "ieigs", "m", "method", "precision", "max_nested", "max_steps", "prec_steps",
         "gradient_steps", "smoother_steps", "lift_e", "center", "wave", "relative")] + [("tol", C.c_double),
-                                                                                  ("smoother", C.c_int)]
+                                                                                  ("smoother", C.c_int),
+                                                                                  ("drop", C.c_double),
+                                                                                  ("extrapolation", C.c_int)]
+
+
+class EpsPattern(C.Structure):
+    """mxg_epspattern (the reference's epspattern, grid2d.h:40-62)."""
+    _fields_ = [("rectangle", C.POINTER(C.c_double)), ("rectangles", C.c_int),
+                ("circle", C.POINTER(C.c_double)), ("circles", C.c_int), ("eps_base", C.c_double)]
 
 
 def lib() -> C.CDLL:
@@ -103,11 +111,38 @@ def lib() -> C.CDLL:
             "mxg_solver_eigenvectors": (I, [P, P]),
             "mxg_solver_stats": (I, [P, P, P]),
             "mxg_solver_profile": (I, [P, I]),
-            "mxg_solver_kernel_time": (I, [P, P, P, P]),
+            "mxg_solver_kernel_time": (I, [P, I, P, P, P]),
             "mxg_eps_sensitivity": (I, [I, P, I, P, P, I, P, P, P]),
             "mxg_device_ok": (I, []),
+            "mxg_set_device": (I, [I]),
+            "mxg_solver_restarts": (I, [P]),
             "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
+            "swap_edge2d_gpu": (I, [P, P]),
+            "random_edge2d_gpu": (I, [P, C.c_ulonglong]),
+            "scale_edge2d_gpu": (I, [Field, P]),
+            "normmax_edge2d_gpu": (I, [P, P]),
+            "dotprod_edge2d_gpu": (I, [P, P, P]),
+            "nullprod_edge2d_gpu": (I, [P, P, P]),
+            "nulladd_edge2d_gpu": (I, [P, P, P]),
+            "gram_edge2d_gpu": (I, [P, P, P]),
+            "lincomb_edge2d_gpu": (I, [P, P, P]),
+            "orthonormalize_edge2d_gpu": (I, [P, P]),
+            "pinvit_edge2d_gpu": (I, [I, I, I, I, P, P, P, P, P, P, P, P, P, P]),
+            "copy_node2d_gpu": (I, [P, P]),
+            "random_node2d_gpu": (I, [P, C.c_ulonglong]),
+            "scale_node2d_gpu": (I, [Field, P]),
+            "add_node2d_gpu": (I, [Field, P, P]),
+            "norm2_node2d_gpu": (I, [P, P]),
+            "normmax_node2d_gpu": (I, [P, P]),
+            "dotprod_node2d_gpu": (I, [P, P, P]),
+            "center_node2d_gpu": (I, [P]),
+            "potrsv_matrix_gpu": (I, [P, P]),
+            "new_epspattern_gpu": (P, [D, I, I]),
+            "del_epspattern_gpu": (None, [P]),
+            "setpattern_grid2d_gpu": (I, [P, P]),
+            "getkappa_grid2d_gpu": (I, [P, P]),
+            "getsize_grid2d_gpu": (I, [P, P, P]),
         }
         for name, (res, args) in protos.items():
             f = getattr(L, name)
@@ -175,6 +210,28 @@ class Grid:
         f = np.asarray(factors, np.complex128).reshape(self.K, 2)
         xf, yf = np.ascontiguousarray(f[:, 0]), np.ascontiguousarray(f[:, 1])
         check(lib().setbloch_grid2d_gpu(self.h, _ptr(xf), _ptr(yf)), "setbloch")
+
+    def set_pattern(self, rects, circles, eps_base=1.0):
+        """setpattern_grid2d_gpu: rectangles (eps, x0, y0, w, h), circles (eps, cx, cy, r)."""
+        rects = np.asarray(rects, np.float64).reshape(-1, 5)
+        circles = np.asarray(circles, np.float64).reshape(-1, 4)
+        p = lib().new_epspattern_gpu(float(eps_base), len(rects), len(circles))
+        if not p:
+            raise RuntimeError("new_epspattern_gpu failed")
+        try:
+            pat = C.cast(p, C.POINTER(EpsPattern)).contents
+            for q, v in enumerate(rects.reshape(-1)):
+                pat.rectangle[q] = v
+            for q, v in enumerate(circles.reshape(-1)):
+                pat.circle[q] = v
+            check(lib().setpattern_grid2d_gpu(p, self.h), "setpattern_grid2d")
+        finally:
+            lib().del_epspattern_gpu(p)
+
+    def kappa(self) -> np.ndarray:
+        k = np.zeros(self.n * self.n)
+        check(lib().getkappa_grid2d_gpu(self.h, _ptr(k)), "getkappa_grid2d")
+        return k
 
     def coarsen(self) -> "Grid":
         h = lib().coarsen_grid2d_gpu(self.h)
@@ -265,9 +322,10 @@ class Solver:
 
     def __init__(self, kappa_fine, *, n0, L, ieigs, m, method=1, precision=1, max_nested=20,
                  max_steps=60, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1, center=1,
-                 wave=1, relative=1, tol=1e-8, smoother=1):
+                 wave=1, relative=1, tol=1e-8, smoother=1, drop=0.0, extrapolation="n"):
         self.o = SolveOpts(n0, L, ieigs, m, method, precision, max_nested, max_steps, prec_steps,
-                           gradient_steps, smoother_steps, lift_e, center, wave, relative, tol, smoother)
+                           gradient_steps, smoother_steps, lift_e, center, wave, relative, tol, smoother, drop,
+                           ord(extrapolation))
         self.n = n0 << L
         self.m, self.wave = m, wave
         k = np.ascontiguousarray(kappa_fine, np.float64)
@@ -307,12 +365,21 @@ class Solver:
         lib().mxg_solver_stats(self.h, C.byref(ms), C.byref(launches))
         return ms.value, launches.value
 
+    def restarts(self) -> int:
+        """Warm-started waves of the last solve that were solved again cold."""
+        return lib().mxg_solver_restarts(self.h)
+
     def profile(self, enable: bool = True):
         check(lib().mxg_solver_profile(self.h, int(enable)), "profile")
 
-    def kernel_time(self):
+    KT_NODE_GS, KT_AFW, KT_GRAM = 0, 1, 2
+
+    def kernel_time(self, which: int = 0):
+        """(summed ms, count, summed algorithmic bytes) of the finest
+        level's node GS sweeps (0), AFW sweeps (1) or Gram launches (2)
+        since profile(True)."""
         ms, cnt, b = C.c_double(0), C.c_long(0), C.c_double(0)
-        check(lib().mxg_solver_kernel_time(self.h, C.byref(ms), C.byref(cnt), C.byref(b)), "kernel_time")
+        check(lib().mxg_solver_kernel_time(self.h, which, C.byref(ms), C.byref(cnt), C.byref(b)), "kernel_time")
         return ms.value, cnt.value, b.value
 
     def __del__(self):

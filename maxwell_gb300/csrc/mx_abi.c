@@ -674,6 +674,11 @@ int sygv_matrix_gpu(matrix_gpu *a, matrix_gpu *b, double *lambda, int *info)
   return e;
 }
 
+int mxg_set_device(int device)
+{
+  return (int) cudaSetDevice(device);
+}
+
 int mxg_device_ok(void)
 {
   int n = 0;
@@ -684,3 +689,386 @@ int mxg_device_ok(void)
 /* accessors for the solver translation unit */
 const double *mxg__grid_phases(const grid2d_gpu *g) { return g->ph; }
 void *mxg__edge_data(const edge2d_gpu *e) { return e->d; }
+
+/* ------------------------------------------------------------------ */
+/* further vector operations of edge2d.h / node2d.h                     */
+/* ------------------------------------------------------------------ */
+
+/* per-(k, vector) complex results of a device reduction into host memory */
+static int reduce_to_host(const grid2d_gpu *g, size_t nd, double **dev)
+{
+  if(cudaMalloc((void **) dev, sizeof(double) * nd)) return MXG_ENOMEM;
+  (void) g;
+  return 0;
+}
+
+int swap_edge2d_gpu(edge2d_gpu *x, edge2d_gpu *y)
+{
+  void *t;
+  if(!same_shape_e(x, y) || x->prec != y->prec) return MXG_EINVAL;
+  TRY((int) cudaStreamSynchronize(x->gr->st));
+  t = x->d; x->d = y->d; y->d = t;
+  return 0;
+}
+
+int random_edge2d_gpu(edge2d_gpu *x, unsigned long long seed)
+{
+  return mxk_random(seed, x->prec, x->d, elen(x), x->gr->st);
+}
+
+int scale_edge2d_gpu(mxg_field alpha, edge2d_gpu *x)
+{
+  return mxk_scale(creal_(alpha), cimag_(alpha), x->prec, x->d, elen(x), x->gr->st);
+}
+
+static int absmax(const grid2d_gpu *g, size_t per, int m, int prec, const void *x, double *out)
+{
+  double *d;
+  int e = reduce_to_host(g, (size_t) g->K * m, &d);
+  if(e) return e;
+  e = mxk_absmax(per, m, g->K, prec, x, d, g->st);
+  if(!e) e = (int) cudaMemcpy(out, d, sizeof(double) * g->K * m, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e;
+}
+
+int normmax_edge2d_gpu(const edge2d_gpu *x, double *out)
+{
+  return absmax(x->gr, 2 * (size_t) x->gr->n * x->gr->n, x->m, x->prec, x->d, out);
+}
+
+int dotprod_edge2d_gpu(const edge2d_gpu *x, const edge2d_gpu *y, mxg_field *out)
+{
+  if(!same_shape_e(x, y) || x->prec != y->prec) return MXG_EINVAL;
+  return dot_e(x, y, (double *) out);
+}
+
+/* both planes' sums per (k, vector): acc[2*((k*2+p)*m+v)] */
+static int plane_sums_e(const edge2d_gpu *x, double *host)
+{
+  const grid2d_gpu *g = x->gr;
+  size_t nd = 2 * (size_t) g->K * 2 * x->m;
+  double *d;
+  int e = reduce_to_host(g, nd, &d);
+  if(e) return e;
+  e = mxk_plane_sums(g->n * g->n, 2, x->m, g->K, x->prec, x->d, d, g->st);
+  if(!e) e = (int) cudaMemcpy(host, d, sizeof(double) * nd, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e;
+}
+
+int nullprod_edge2d_gpu(const edge2d_gpu *x, mxg_field *xprod, mxg_field *yprod)
+{
+  /* edge2d.c:1240-1274: xprod = hx * sum 6 mx x = hy * sum of the x plane,
+   * yprod = hx * sum of the y plane (hx = hy = 1/n) */
+  const grid2d_gpu *g = x->gr;
+  size_t km = (size_t) g->K * x->m, q;
+  double *s = malloc(sizeof(double) * 4 * km), h = g->h;
+  int e;
+  if(!s) return MXG_ENOMEM;
+  e = plane_sums_e(x, s);
+  for(q = 0; !e && q < km; q++) {
+    size_t k = q / x->m, v = q % x->m;
+    const double *sx = s + 2 * ((k * 2 + 0) * x->m + v), *sy = s + 2 * ((k * 2 + 1) * x->m + v);
+    if(xprod) { double *o = (double *) (xprod + q); o[0] = h * sx[0]; o[1] = h * sx[1]; }
+    if(yprod) { double *o = (double *) (yprod + q); o[0] = h * sy[0]; o[1] = h * sy[1]; }
+  }
+  free(s);
+  return e;
+}
+
+int nulladd_edge2d_gpu(const mxg_field *xalpha, const mxg_field *yalpha, edge2d_gpu *x)
+{
+  /* edge2d.c:1276-1307: x plane += hx xalpha, y plane += hy yalpha */
+  const grid2d_gpu *g = x->gr;
+  size_t km = (size_t) g->K * x->m, q, nd = 4 * km;
+  double *c = malloc(sizeof(double) * nd), *d;
+  int e;
+  if(!c) return MXG_ENOMEM;
+  for(q = 0; q < km; q++) {
+    size_t k = q / x->m, v = q % x->m;
+    double *cx = c + 2 * ((k * 2 + 0) * x->m + v), *cy = c + 2 * ((k * 2 + 1) * x->m + v);
+    cx[0] = creal_(xalpha[q]); cx[1] = cimag_(xalpha[q]);
+    cy[0] = creal_(yalpha[q]); cy[1] = cimag_(yalpha[q]);
+  }
+  e = reduce_to_host(g, nd, &d);
+  if(!e) {
+    e = (int) cudaMemcpy(d, c, sizeof(double) * nd, cudaMemcpyHostToDevice);
+    if(!e) e = mxk_plane_shift(g->n * g->n, 2, x->m, g->K, d, g->h, x->prec, x->d, g->st);
+    if(!e) e = (int) cudaStreamSynchronize(g->st);
+    cudaFree(d);
+  }
+  free(c);
+  return e;
+}
+
+/* Block Gram of the m vectors of every k-point: a[k] = X^H (A+M) X and
+ * m[k] = X^H M X, full Hermitian m x m, column-major */
+static int gram_e(const edge2d_gpu *x, double *ga, double *gm)
+{
+  const grid2d_gpu *g = x->gr;
+  int pr[1];
+  const void *pp[1];
+  size_t nent = (size_t) x->m * (x->m + 1) / 2;
+  size_t scratch = (size_t) g->K * 256 * nent * 4 * sizeof(double);
+  double *sc;
+  int e;
+  if(scratch > ((size_t) 1 << 28)) scratch = (size_t) 1 << 28;
+  if(cudaMalloc((void **) &sc, scratch)) return MXG_ENOMEM;
+  pr[0] = x->prec; pp[0] = x->d;
+  e = mxk_block_gram(g->n, x->m, g->K, g->ph, kap_of(g), 1, pr, pp, 0, 0, ga, gm, sc, scratch, g->st);
+  if(!e) e = (int) cudaStreamSynchronize(g->st);
+  cudaFree(sc);
+  return e;
+}
+
+int gram_edge2d_gpu(const edge2d_gpu *x, mxg_field *a, mxg_field *m)
+{
+  const grid2d_gpu *g = x->gr;
+  size_t sz = sizeof(double) * 2 * (size_t) x->m * x->m * g->K;
+  double *ga, *gm;
+  int e;
+  if(x->m > 48) return MXG_EINVAL;
+  if(cudaMalloc((void **) &ga, sz)) return MXG_ENOMEM;
+  if(cudaMalloc((void **) &gm, sz)) { cudaFree(ga); return MXG_ENOMEM; }
+  e = gram_e(x, ga, gm);
+  if(!e && a) e = (int) cudaMemcpy(a, ga, sz, cudaMemcpyDeviceToHost);
+  if(!e && m) e = (int) cudaMemcpy(m, gm, sz, cudaMemcpyDeviceToHost);
+  cudaFree(ga);
+  cudaFree(gm);
+  return e;
+}
+
+/* y[k][j] = sum_i coef[k](i, j) x[k][i] */
+static int lincomb_dev(const edge2d_gpu *x, const double *dcoef, edge2d_gpu *y)
+{
+  const grid2d_gpu *g = x->gr;
+  int pr[1];
+  const void *pp[1];
+  void *cw;
+  int e;
+  if(cudaMalloc(&cw, (size_t) 16 * x->m * x->m * g->K)) return MXG_ENOMEM;
+  pr[0] = x->prec; pp[0] = x->d;
+  e = mxk_block_combine(g->n, x->m, g->K, 1, pr, pp, dcoef, x->m, 0, cw, y->prec, y->d, g->st);
+  if(!e) e = (int) cudaStreamSynchronize(g->st);
+  cudaFree(cw);
+  return e;
+}
+
+int lincomb_edge2d_gpu(const mxg_field *coef, const edge2d_gpu *x, edge2d_gpu *y)
+{
+  size_t sz = sizeof(double) * 2 * (size_t) x->m * x->m * x->gr->K;
+  double *d;
+  int e;
+  if(!same_shape_e(x, y) || x == y || x->d == y->d) return MXG_EINVAL;
+  if(cudaMalloc((void **) &d, sz)) return MXG_ENOMEM;
+  e = (int) cudaMemcpy(d, coef, sz, cudaMemcpyHostToDevice);
+  if(!e) e = lincomb_dev(x, d, y);
+  cudaFree(d);
+  return e;
+}
+
+int orthonormalize_edge2d_gpu(edge2d_gpu *x, int *info)
+{
+  /* Cholesky-QR in the mass inner product: G = X^H M X = R^H R, X <- X R^-1 */
+  const grid2d_gpu *g = x->gr;
+  size_t sz = sizeof(double) * 2 * (size_t) x->m * x->m * g->K;
+  double *ga = 0, *gm = 0, *coef = 0;
+  int *dinfo = 0, e, k, bad = 0;
+  edge2d_gpu *t;
+  if(x->m > 48) return MXG_EINVAL;
+  t = new_edge2d_gpu(g, x->m, x->prec);
+  if(!t) return MXG_ENOMEM;
+  if(cudaMalloc((void **) &ga, sz) || cudaMalloc((void **) &gm, sz) || cudaMalloc((void **) &coef, sz)
+     || cudaMalloc((void **) &dinfo, sizeof(int) * g->K)) {
+    e = MXG_ENOMEM;
+    goto out;
+  }
+  e = gram_e(x, ga, gm);
+  if(!e) e = mxk_chol_qr_coef(x->m, g->K, gm, coef, dinfo, g->st);
+  if(!e) e = (int) cudaMemcpy(info, dinfo, sizeof(int) * g->K, cudaMemcpyDeviceToHost);
+  for(k = 0; !e && k < g->K; k++)
+    if(info[k]) bad = 1;
+  if(!e && !bad) e = lincomb_dev(x, coef, t);
+  if(!e && !bad) { void *q = x->d; x->d = t->d; t->d = q; }
+  if(!e && bad) e = MXG_ECONV;
+out:
+  cudaFree(ga); cudaFree(gm); cudaFree(coef); cudaFree(dinfo);
+  del_edge2d_gpu(t);
+  return e;
+}
+
+int pinvit_edge2d_gpu(int l, int smoother_steps, int prec_steps, int gradient_steps, const double *lambda,
+                      edge2d_gpu *e, const matrix_gpu *Ae, edge2d_gpu **b, edge2d_gpu **x, edge2d_gpu **d,
+                      const matrix_gpu *An, node2d_gpu **bg, node2d_gpu **xg, node2d_gpu **dg)
+{
+  /* pinvit_edge2d (edge2d.c:6298-6328) for every (k, vector) of the batch,
+   * each with its own lambda (the defect is (A+M) e - lambda M e) */
+  const grid2d_gpu *g = e->gr;
+  size_t km = (size_t) g->K * e->m, q;
+  double *shift = malloc(sizeof(double) * km);
+  int j, err;
+  if(!shift) return MXG_ENOMEM;
+  for(q = 0; q < km; q++) shift[q] = 1.0 - lambda[q];
+  err = zero_edge2d_gpu(b[l]);
+  if(!err) err = addeval_shifted_edge2d_gpu(1.0, shift, e, b[l]);
+  free(shift);
+  if(!err) err = zero_edge2d_gpu(x[l]);
+  for(j = 0; !err && j < prec_steps; j++) err = vcycle_edge2d_gpu(l, smoother_steps, Ae, b, x, d);
+  if(!err) err = add_edge2d_gpu(-1.0, x[l], e);
+  if(!err) err = zero_edge2d_gpu(d[l]);
+  if(!err) err = addeval_edge2d_gpu(0.0, 1.0, e, d[l]);
+  if(!err) err = zero_node2d_gpu(bg[l]);
+  if(!err) err = adjgradient_node2d_gpu(1.0, d[l], bg[l]);
+  if(!err) err = zero_node2d_gpu(xg[l]);
+  for(j = 0; !err && j < gradient_steps; j++) err = vcycle_node2d_gpu(l, smoother_steps, An, bg, xg, dg);
+  if(!err) err = gradient_node2d_gpu(-1.0, xg[l], e);
+  if(!err) err = (int) cudaStreamSynchronize(g->st);
+  return err;
+}
+
+int copy_node2d_gpu(const node2d_gpu *x, node2d_gpu *y)
+{
+  if(x->gr->n != y->gr->n || x->gr->K != y->gr->K || x->m != y->m) return MXG_EINVAL;
+  return mxk_convert(x->prec, x->d, y->prec, y->d, nlen(x), x->gr->st);
+}
+
+int random_node2d_gpu(node2d_gpu *x, unsigned long long seed)
+{
+  return mxk_random(seed, x->prec, x->d, nlen(x), x->gr->st);
+}
+
+int scale_node2d_gpu(mxg_field alpha, node2d_gpu *x)
+{
+  return mxk_scale(creal_(alpha), cimag_(alpha), x->prec, x->d, nlen(x), x->gr->st);
+}
+
+int add_node2d_gpu(mxg_field alpha, const node2d_gpu *x, node2d_gpu *y)
+{
+  if(x->gr->n != y->gr->n || x->gr->K != y->gr->K || x->m != y->m) return MXG_EINVAL;
+  return mxk_axpy(creal_(alpha), cimag_(alpha), x->prec, x->d, y->prec, y->d, nlen(x), x->gr->st);
+}
+
+static int dot_n(const node2d_gpu *x, const node2d_gpu *y, double *out)
+{
+  double *d;
+  int e;
+  size_t km = (size_t) x->gr->K * x->m;
+  if(cudaMalloc((void **) &d, sizeof(double) * 2 * km)) return MXG_ENOMEM;
+  e = (int) cudaMemsetAsync(d, 0, sizeof(double) * 2 * km, x->gr->st);
+  if(!e) e = mxk_dot((size_t) x->gr->n * x->gr->n, x->m, x->gr->K, x->prec, x->d, y->prec, y->d, d, x->gr->st);
+  if(!e) e = (int) cudaMemcpy(out, d, sizeof(double) * 2 * km, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e;
+}
+
+int dotprod_node2d_gpu(const node2d_gpu *x, const node2d_gpu *y, mxg_field *out)
+{
+  if(x->gr->n != y->gr->n || x->gr->K != y->gr->K || x->m != y->m || x->prec != y->prec) return MXG_EINVAL;
+  return dot_n(x, y, (double *) out);
+}
+
+int norm2_node2d_gpu(const node2d_gpu *x, double *out)
+{
+  size_t km = (size_t) x->gr->K * x->m, i;
+  double *t = malloc(sizeof(double) * 2 * km);
+  int e;
+  if(!t) return MXG_ENOMEM;
+  e = dot_n(x, x, t);
+  for(i = 0; !e && i < km; i++) out[i] = sqrt(t[2 * i]);
+  free(t);
+  return e;
+}
+
+int normmax_node2d_gpu(const node2d_gpu *x, double *out)
+{
+  return absmax(x->gr, (size_t) x->gr->n * x->gr->n, x->m, x->prec, x->d, out);
+}
+
+int center_node2d_gpu(node2d_gpu *x)
+{
+  /* node2d.c:489-514: subtract the mean of the n*n coefficients */
+  const grid2d_gpu *g = x->gr;
+  size_t nd = 2 * (size_t) g->K * x->m;
+  double *d;
+  int e = reduce_to_host(g, nd, &d);
+  if(e) return e;
+  e = mxk_plane_sums(g->n * g->n, 1, x->m, g->K, x->prec, x->d, d, g->st);
+  if(!e) e = mxk_plane_shift(g->n * g->n, 1, x->m, g->K, d, -1.0 / ((double) g->n * g->n), x->prec, x->d, g->st);
+  if(!e) e = (int) cudaStreamSynchronize(g->st);
+  cudaFree(d);
+  return e;
+}
+
+int potrsv_matrix_gpu(const matrix_gpu *a, mxg_field *b)
+{
+  /* potrsv_matrix (linalg.c:98-113): b <- A^-1 b per k, with the factor of
+   * potrf_matrix_gpu (kept as the explicit inverse) */
+  size_t sz = sizeof(double) * 2 * (size_t) a->rows * a->K;
+  double *x, *y;
+  int e;
+  if(!a->factored) return MXG_EINVAL;
+  if(cudaMalloc((void **) &x, sz)) return MXG_ENOMEM;
+  if(cudaMalloc((void **) &y, sz)) { cudaFree(x); return MXG_ENOMEM; }
+  e = (int) cudaMemcpy(x, b, sz, cudaMemcpyHostToDevice);
+  if(!e) e = mxk_coarse_apply(a->rows, 1, a->K, a->d, 0, MX_C128, x, y, 0);
+  if(!e) e = (int) cudaMemcpy(b, y, sz, cudaMemcpyDeviceToHost);
+  cudaFree(x);
+  cudaFree(y);
+  return e;
+}
+
+/* ------------------------------------------------------------------ */
+/* permittivity patterns (grid2d.h:40-78)                               */
+/* ------------------------------------------------------------------ */
+
+mxg_epspattern *new_epspattern_gpu(double eps_base, int rectangles, int circles)
+{
+  mxg_epspattern *p;
+  if(rectangles < 0 || circles < 0) return 0;
+  p = calloc(1, sizeof(mxg_epspattern));
+  if(!p) return 0;
+  p->rectangle = calloc((size_t) 5 * rectangles + 1, sizeof(double));
+  p->circle = calloc((size_t) 4 * circles + 1, sizeof(double));
+  p->rectangles = rectangles;
+  p->circles = circles;
+  p->eps_base = eps_base;
+  if(!p->rectangle || !p->circle) { del_epspattern_gpu(p); return 0; }
+  return p;
+}
+
+void del_epspattern_gpu(mxg_epspattern *p)
+{
+  if(!p) return;
+  free(p->rectangle);
+  free(p->circle);
+  free(p);
+}
+
+int setpattern_grid2d_gpu(const mxg_epspattern *pat, grid2d_gpu *g)
+{
+  size_t nn = (size_t) g->n * g->n;
+  double *rect = 0, *circ = 0, *kd = 0;
+  int e;
+  if(!pat) return 0;   /* setpattern_grid2d returns without a pattern */
+  if(pat->rectangles < 0 || pat->circles < 0) return MXG_EINVAL;
+  if(cudaMalloc((void **) &rect, sizeof(double) * (5 * (size_t) pat->rectangles + 1))
+     || cudaMalloc((void **) &circ, sizeof(double) * (4 * (size_t) pat->circles + 1))
+     || cudaMalloc((void **) &kd, sizeof(double) * nn)) {
+    cudaFree(rect); cudaFree(circ);
+    return MXG_ENOMEM;
+  }
+  e = (int) cudaMemcpy(rect, pat->rectangle, sizeof(double) * 5 * pat->rectangles, cudaMemcpyHostToDevice);
+  if(!e) e = (int) cudaMemcpy(circ, pat->circle, sizeof(double) * 4 * pat->circles, cudaMemcpyHostToDevice);
+  if(!e) e = mxk_pattern(g->n, rect, pat->rectangles, circ, pat->circles, pat->eps_base, kd, g->st);
+  if(!e) e = (int) cudaMemcpy(g->h_kappa, kd, sizeof(double) * nn, cudaMemcpyDeviceToHost);
+  if(!e) e = upload_kappa(g);
+  cudaFree(rect); cudaFree(circ); cudaFree(kd);
+  return e;
+}
+
+int getkappa_grid2d_gpu(const grid2d_gpu *g, double *kappa)
+{
+  memcpy(kappa, g->h_kappa, sizeof(double) * g->n * g->n);
+  return 0;
+}

@@ -608,3 +608,66 @@ extern "C" int mxk_rayleigh_ritz(int ns, int m, int K, const double* ga, const d
   MX_CHECK_LAUNCH();
   return 0;
 }
+
+// ------------------------------------------------------------------
+// Cholesky-QR coefficients: for the Hermitian positive definite mass Gram
+// G = X^H M X of m vectors, G = R^H R with R upper triangular and a positive
+// real diagonal, and coef = R^{-1}; X coef is then M-orthonormal and its
+// first j columns span the first j columns of X (the function of the
+// reference's Householder orthonormalisation, orthonormalize_edge2d,
+// edge2d.c:6264-6296).  info[k] = 0, or j+1 if column j is (numerically)
+// dependent on the columns before it.
+// ------------------------------------------------------------------
+namespace {
+__global__ void k_chol_qr_coef(int m, const double* __restrict__ gm, double* __restrict__ coef, int* info) {
+  extern __shared__ double smc[];
+  Z* R = reinterpret_cast<Z*>(smc);          // m x m column-major
+  __shared__ int bad;
+  const double* G = gm + (size_t) blockIdx.x * 2 * m * m;
+  double* C = coef + (size_t) blockIdx.x * 2 * m * m;
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) R[e] = reinterpret_cast<const Z*>(G)[e];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < m; j++) {
+    // row j of R: R_jj = sqrt(G_jj - sum |R_ij|^2), R_jc = (G_jc - sum conj(R_ij) R_ic) / R_jj
+    __shared__ double djj;
+    if (threadIdx.x == 0) {
+      double g = R[j * m + j].re, d = g;
+      for (int i = 0; i < j; i++) d -= zabs2(R[j * m + i]);
+      // column j counts as dependent when the part of it outside the span
+      // of the columns before it has less than 1e-5 of its M-norm
+      if (!(d > 1e-10 * g) && !bad) bad = j + 1;
+      djj = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    for (int c = j + 1 + threadIdx.x; c < m; c += blockDim.x) {
+      Z s = R[c * m + j];
+      for (int i = 0; i < j; i++) s = zsub(s, zcmul(R[j * m + i], R[c * m + i]));
+      R[c * m + j] = zscal(1.0 / djj, s);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) R[j * m + j] = zmk(djj, 0.0);
+    __syncthreads();
+  }
+  // coef = R^{-1}, one column per thread (back substitution)
+  for (int c = threadIdx.x; c < m; c += blockDim.x) {
+    for (int i = m - 1; i > c; i--) AT(C, m, i, c) = zmk(0.0, 0.0);
+    AT(C, m, c, c) = zmk(1.0 / R[c * m + c].re, 0.0);
+    for (int i = c - 1; i >= 0; i--) {
+      Z s = zmk(0.0, 0.0);
+      for (int q = i + 1; q <= c; q++) s = zadd(s, zmul(R[q * m + i], AT(C, m, q, c)));
+      AT(C, m, i, c) = zscal(-1.0 / R[i * m + i].re, s);
+    }
+  }
+  if (threadIdx.x == 0 && info) info[blockIdx.x] = bad;
+}
+}  // namespace
+
+extern "C" int mxk_chol_qr_coef(int m, int K, const double* gm, double* coef, int* info, mx_stream s) {
+  if (m < 1 || m > 64) return (int) cudaErrorInvalidValue;
+  size_t smem = sizeof(double) * 2 * (size_t) m * m;
+  cudaFuncSetAttribute(k_chol_qr_coef, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  k_chol_qr_coef<<<K, 64, smem, (cudaStream_t) s>>>(m, gm, coef, info);
+  MX_CHECK_LAUNCH();
+  return 0;
+}

@@ -91,6 +91,23 @@ int mxk_dot(size_t per, int m, int K, int prec_x, const void *x, int prec_y, con
  * only applied to k-points whose flag is set.  acc: 4*K*m doubles of scratch. */
 int mxk_center(int n, int m, int K, const int *gamma_flag, int prec, void *x, double *acc, mx_stream s);
 
+/* ---- further vector operations (mx_vec.cu) ---- */
+/* x *= alpha over len complex entries */
+int mxk_scale(double are, double aim, int prec, void *x, size_t len, mx_stream s);
+/* uniform re and im in [-1, 1) from a counter-based generator keyed by seed */
+int mxk_random(unsigned long long seed, int prec, void *x, size_t len, mx_stream s);
+/* out[k*m+v] = max |x| over the `per` entries of each (k, v) */
+int mxk_absmax(size_t per, int m, int K, int prec, const void *x, double *out, mx_stream s);
+/* acc[2*((k*planes+p)*m+v)] = sum of plane p (nsite entries) of (k, v), (re, im) */
+int mxk_plane_sums(int nsite, int planes, int m, int K, int prec, const void *x, double *acc, mx_stream s);
+/* plane p of (k, v) += scale * c[2*((k*planes+p)*m+v)] */
+int mxk_plane_shift(int nsite, int planes, int m, int K, const double *c, double scale, int prec, void *x,
+                    mx_stream s);
+/* kappa (n*n device doubles) from rectangles (eps, x0, y0, w, h) and circles
+ * (eps, cx, cy, r) in device memory, setpattern_grid2d's rule */
+int mxk_pattern(int n, const double *rect, int nrect, const double *circ, int ncirc, double eps_base,
+                double *kappa, mx_stream s);
+
 /* ---- coarse dense matrices (one per k, column-major, complex double) ---- */
 /* A = alpha*A + beta*M on the 2n^2 edges of level 0 */
 int mxk_dense_edge(int n, int K, const double *phases, mxk_kappa kap, double alpha,
@@ -120,6 +137,10 @@ size_t mxk_ritz_work_doubles(int ns);
 int mxk_rayleigh_ritz(int ns, int m, int K, const double *ga, const double *gm,
                       const int *sel, double drop, double theta_min, double *coef, double *theta,
                       int *info, double *work, mx_stream s);
+
+/* Cholesky-QR coefficients: gm (K Hermitian m x m mass Gram matrices) =
+ * R^H R, coef = R^{-1} (upper triangular); info[k] = j+1 at a non-positive pivot */
+int mxk_chol_qr_coef(int m, int K, const double *gm, double *coef, int *info, mx_stream s);
 
 /* ---- block (eigenvector) kernels ---- */
 /* For every (k,v): W = (A+M) e, V = M e (arithmetic of prec_e);

@@ -59,7 +59,8 @@ struct mxg_solver {
   void *bg[MAXL], *xg[MAXL], *dg[MAXL];
   double *ae_inv, *an_inv;
   void *ae_inv_f, *an_inv_f;         /* their c64 roundings (FP32 solves) */
-  void *E, *En, *P, *Pn, *Eprev;
+  void *E, *En, *P, *Pn;
+  void *Eprev[3];                    /* eigenvectors of the last three waves, newest first */
   double *ga, *gm, *coef, *theta, *rwork, *gscratch, *mu, *stats;
   size_t gscratch_bytes;
   int *sel, *info;
@@ -70,18 +71,22 @@ struct mxg_solver {
   /* host */
   double *h_ph, *h_stats, *h_mu, *h_res, *h_rq;
   int *h_sel, *h_info, *h_conv, *h_steps;
-  int have_prev, K_prev;
+  int have_prev, K_prev;              /* waves stored in Eprev (0..3) and their width */
   double last_ms;
   long launches;
-  /* CUDA-event timing of the finest-level AFW sweeps (the dominant kernel) */
+  /* CUDA-event timing of the finest level's node Gauss-Seidel sweeps, AFW
+   * sweeps and Gram launches (mxg_solver_profile): event pairs on the
+   * solver's stream, each with its kernel kind and algorithmic bytes */
   int timing;
   cudaEvent_t tev[PH_N + 1];
   double tph[PH_N];
   int prof;
   cudaEvent_t *pev;
+  int *ptag;
+  double *pbytes;
   int npev, maxpev;
-  double prof_ms;
-  long prof_count;
+  double prof_ms[MXG_KT_N], prof_bytes[MXG_KT_N];
+  long prof_count[MXG_KT_N];
   int prof_step, prof_done;          /* profiler window (MXG_PROFILE_STEP) */
   /* CUDA graphs of the inner multigrid loops, one per level: the edge
    * V-cycles of the preconditioner and the node V-cycles of a lifting */
@@ -89,6 +94,9 @@ struct mxg_solver {
   long gpre_n[MAXL], glift_n[MAXL];   /* kernel launches each graph holds */
   int graphs;                          /* 1 capture and replay, 0 launch directly */
   int restarts;                       /* warm-started waves solved again cold */
+  int debug;                          /* per-step residual trace on stderr */
+  int order;                          /* earlier waves a warm start combines (1, 2 or 3) */
+  int device;                         /* the CUDA device the solver lives on */
 };
 
 #define L_(x) do { int e_ = (x); s->launches++; if (e_) return e_; } while (0)
@@ -122,7 +130,8 @@ void mxg_solver_free(mxg_solver *s)
     cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
   }
   cudaFree(s->ph); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv); cudaFree(s->ae_inv_f); cudaFree(s->an_inv_f);
-  cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn); cudaFree(s->Eprev);
+  cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn);
+  cudaFree(s->Eprev[0]); cudaFree(s->Eprev[1]); cudaFree(s->Eprev[2]);
   cudaFree(s->ga); cudaFree(s->gm); cudaFree(s->coef); cudaFree(s->theta); cudaFree(s->rwork);
   cudaFree(s->gscratch); cudaFree(s->mu); cudaFree(s->stats); cudaFree(s->sel); cudaFree(s->info);
   cudaFree(s->cA); cudaFree(s->cM); cudaFree(s->ccoef); cudaFree(s->ctheta); cudaFree(s->cwork);
@@ -133,6 +142,8 @@ void mxg_solver_free(mxg_solver *s)
     int q;
     for(q = 0; q < s->maxpev; q++) cudaEventDestroy(s->pev[q]);
     free(s->pev);
+    free(s->ptag);
+    free(s->pbytes);
   }
   if(s->st) cudaStreamDestroy(s->st);
   if(s->ev0) cudaEventDestroy(s->ev0);
@@ -149,10 +160,13 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   size_t es_g, es_e;
   double *kk[MAXL];
   if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 16
-     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 1)
+     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 1
+     || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'))
     return 0;
   s = calloc(1, sizeof(mxg_solver));
   s->o = *o;
+  s->order = o->extrapolation == '2' ? 3 : o->extrapolation == '1' ? 2 : 1;
+  if(cudaGetDevice(&s->device) != cudaSuccess) { free(s); return 0; }
   s->n0 = o->n0; s->L = o->L; s->m = m = o->m; s->K = K = o->wave;
   s->pe = o->precision ? MX_CDD : MX_C128;
   s->pg = o->precision ? MX_C64 : MX_C128;
@@ -210,7 +224,9 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
      || dalloc(&s->ae_inv_f, sizeof(float) * 2 * (size_t) N0e * N0e * K)
      || dalloc(&s->an_inv_f, sizeof(float) * 2 * (size_t) N0n * N0n * K)
      || dalloc(&s->E, elen(s, o->L) * es_e) || dalloc(&s->En, elen(s, o->L) * es_e)
-     || dalloc(&s->Eprev, elen(s, o->L) * es_e)
+     || dalloc(&s->Eprev[0], elen(s, o->L) * es_e)
+     || (s->order > 1 && dalloc(&s->Eprev[1], elen(s, o->L) * es_e))
+     || (s->order > 2 && dalloc(&s->Eprev[2], elen(s, o->L) * es_e))
      || dalloc(&s->P, elen(s, o->L) * es_g) || dalloc(&s->Pn, elen(s, o->L) * es_g)
      || dalloc((void **) &s->ga, sizeof(double) * 2 * ns * ns * K) || dalloc((void **) &s->gm, sizeof(double) * 2 * ns * ns * K)
      || dalloc((void **) &s->coef, sizeof(double) * 2 * ns * m * K) || dalloc((void **) &s->theta, sizeof(double) * m * K)
@@ -238,8 +254,10 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   s->h_info = malloc(sizeof(int) * K);
   s->h_conv = malloc(sizeof(int) * K);
   s->h_steps = malloc(sizeof(int) * K);
+  /* diagnostics only, read once here: none of them changes a result */
   s->timing = getenv("MXG_TIMING") != 0;
   s->graphs = getenv("MXG_NO_GRAPHS") == 0;
+  s->debug = getenv("MXG_DEBUG") != 0;
   /* MXG_PROFILE_STEP=q brackets finest-level block step q of the first wave
    * with cudaProfilerStart/Stop, for a profiler started with profiling off */
   s->prof_step = getenv("MXG_PROFILE_STEP") ? atoi(getenv("MXG_PROFILE_STEP")) : -1;
@@ -255,6 +273,13 @@ fail:
 
 /* ------------------------------------------------------------------ */
 
+/* k = 0 up to rounding: the same rule as the coarse node matrix's fixnull
+ * shift (|xf - 1| + |yf - 1| < 1e-8 in the 1-norm of the components) */
+static int is_gamma(mxg_field xf, mxg_field yf)
+{
+  return fabs(creal(xf) - 1.0) + fabs(cimag(xf)) + fabs(creal(yf) - 1.0) + fabs(cimag(yf)) < 1e-8;
+}
+
 static int set_bloch(mxg_solver *s, int K, const mxg_field *xf, const mxg_field *yf)
 {
   int k, *g = malloc(sizeof(int) * s->K), e;
@@ -262,7 +287,7 @@ static int set_bloch(mxg_solver *s, int K, const mxg_field *xf, const mxg_field 
     int q = k < K ? k : K - 1;   /* unused slots repeat the last k-point */
     s->h_ph[4 * k] = creal(xf[q]); s->h_ph[4 * k + 1] = cimag(xf[q]);
     s->h_ph[4 * k + 2] = creal(yf[q]); s->h_ph[4 * k + 3] = cimag(yf[q]);
-    g[k] = xf[q] == 1.0 && yf[q] == 1.0;
+    g[k] = is_gamma(xf[q], yf[q]);
   }
   mxk_phase_fill(s->K, s->h_ph);
   e = (int) cudaMemcpyAsync(s->ph, s->h_ph, mxk_phase_bytes(s->K), cudaMemcpyHostToDevice, s->st);
@@ -300,28 +325,55 @@ static void prof_flush(mxg_solver *s)
   cudaEventSynchronize(s->pev[s->npev > 0 ? s->npev - 1 : 0]);
   for(q = 0; q + 1 < s->npev; q += 2) {
     float ms = 0.0f;
+    int t = s->ptag[q / 2];
     cudaEventElapsedTime(&ms, s->pev[q], s->pev[q + 1]);
-    s->prof_ms += ms;
-    s->prof_count++;
+    s->prof_ms[t] += ms;
+    s->prof_bytes[t] += s->pbytes[q / 2];
+    s->prof_count[t]++;
   }
   s->npev = 0;
 }
 
-/* one AFW sweep; the finest level's sweeps are timed when profiling is on */
+/* brackets one launch sequence of kind `tag` at the finest level with a pair
+ * of events when profiling is on; prof_end closes the pair */
+static int prof_begin(mxg_solver *s, int l, int tag, double bytes)
+{
+  if(!s->prof || l != s->L) return 0;
+  if(s->npev + 2 > s->maxpev) prof_flush(s);
+  s->ptag[s->npev / 2] = tag;
+  s->pbytes[s->npev / 2] = bytes;
+  cudaEventRecord(s->pev[s->npev++], s->st);
+  return 1;
+}
+static void prof_end(mxg_solver *s, int on)
+{
+  if(on) cudaEventRecord(s->pev[s->npev++], s->st);
+}
+
+/* one AFW sweep: x, b read once, x written once, kappa and the patch
+ * factor table read once */
 static int edge_gs(mxg_solver *s, int l, int dir)
 {
-  int timed = s->prof && l == s->L;
+  double nn = (double) s->n[l] * s->n[l];
+  int on = prof_begin(s, l, MXG_KT_AFW, (double) elen(s, l) * 3.0 * mxk_elem_size(s->pg) + 36.0 * nn);
   int e;
-  if(timed) {
-    if(s->npev + 2 > s->maxpev) prof_flush(s);
-    cudaEventRecord(s->pev[s->npev++], s->st);
-  }
   if(s->o.smoother)
     e = mxk_edge_gs_colour(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
   else
     e = mxk_edge_gs(s->n[l], s->m, s->K, s->ph, kap(s, l), 1.0, 1.0, dir, s->pg, s->b[l], s->x[l], s->st);
   s->launches += 2 * (dir == 2 ? 2 : 1);
-  if(timed) cudaEventRecord(s->pev[s->npev++], s->st);
+  prof_end(s, on);
+  return e;
+}
+
+/* one node Gauss-Seidel sweep (four row-group launches): x, b read once,
+ * x written once */
+static int node_gs(mxg_solver *s, int l, int dir)
+{
+  int on = prof_begin(s, l, MXG_KT_NODE_GS, (double) nlen(s, l) * 3.0 * mxk_elem_size(s->pg));
+  int e = mxk_node_gs(s->n[l], s->m, s->K, s->ph, 1.0, dir, s->pg, s->bg[l], s->xg[l], s->st);
+  s->launches += 4;
+  prof_end(s, on);
   return e;
 }
 
@@ -354,10 +406,8 @@ static int vcycle_n(mxg_solver *s, int top)
   int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
   for(l = top; l > 0; l--) {
     int n = s->n[l];
-    for(i = 0; i < nu; i++) {
-      L_(mxk_node_gs(n, m, K, s->ph, 1.0, 0, pg, s->bg[l], s->xg[l], s->st));
-      s->launches += 3;   /* four row groups */
-    }
+    for(i = 0; i < nu; i++)
+      TRY(node_gs(s, l, 0));
     L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->bg[l], s->dg[l], s->st));
     L_(mxk_zero(pg, s->bg[l - 1], nlen(s, l - 1), s->st));
     L_(mxk_node_restrict(n / 2, m, K, s->ph, 1.0, pg, s->dg[l], s->bg[l - 1], s->st));
@@ -367,10 +417,8 @@ static int vcycle_n(mxg_solver *s, int top)
   for(l = 1; l <= top; l++) {
     int n = s->n[l];
     L_(mxk_node_prolong(n / 2, m, K, s->ph, 1.0, pg, s->xg[l - 1], s->xg[l], s->st));
-    for(i = 0; i < nu; i++) {
-      L_(mxk_node_gs(n, m, K, s->ph, 1.0, 1, pg, s->bg[l], s->xg[l], s->st));
-      s->launches += 3;
-    }
+    for(i = 0; i < nu; i++)
+      TRY(node_gs(s, l, 1));
   }
   return 0;
 }
@@ -498,9 +546,15 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
   /* the residual of E sits in b[l] (written by residual()) with the Ritz
    * values mu; the mixed solver forms the E-to-search-block entries from it */
   const void *rr = (s->pe == MX_CDD && nb > 1) ? s->b[l] : 0;
-  int tm = s->timing && l == s->L && nb > 1;
+  int tm = s->timing && l == s->L && nb > 1, on, b;
+  double gbytes = 12.0 * s->n[l] * s->n[l];   /* kappa as float and float-float pair */
+  for(b = 0; b < nb; b++) gbytes += (double) elen(s, l) * mxk_elem_size(pr[b]);
+  if(rr) gbytes += (double) elen(s, l) * 8.0;
+  on = prof_begin(s, l, MXG_KT_GRAM, gbytes);
   L_(mxk_block_gram(s->n[l], m, K, s->ph, kap(s, l), nb, pr, pp, rr, s->mu, s->ga, s->gm, s->gscratch,
                     s->gscratch_bytes, s->st));
+  s->launches++;   /* the reduction of the partial sums */
+  prof_end(s, on);
   for(k = 0; k < K; k++)
     for(j = 0; j < nb; j++)
       for(i = 0; i < m; i++)
@@ -523,10 +577,11 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
   return upload_mu(s);
 }
 
+/* pivot^2 below which Cholesky-QR drops a column of the Ritz basis
+ * (mxg_solve_opts.drop, or the default of the precision) */
 static double drop_tol(const mxg_solver *s)
 {
-  const char *e = getenv("MXG_DROP");
-  if(e) return atof(e);
+  if(s->o.drop > 0.0) return s->o.drop;
   return s->o.precision ? 1e-6 : 1e-12;
 }
 
@@ -606,7 +661,7 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
       }
       cudaGetLastError();
     }
-    if(getenv("MXG_DEBUG")) {
+    if(s->debug) {
       int i;
       fprintf(stderr, "level %d step %d rank %d:", l, step, s->h_info[0]);
       for(i = 0; i < s->m; i++) fprintf(stderr, " %.1e", s->h_res[i]);
@@ -688,12 +743,53 @@ static int cold_start(mxg_solver *s, int K_active)
   return 0;
 }
 
+/* The start block of a warm-started wave.  With np = min(order, stored
+ * waves) > 1 it is the Rayleigh-Ritz extrapolation of exp_bloch2d.c:814-895
+ * ('1': np = 2, '2': np = 3): Gram matrices of the basis [E_{w-1} .. E_{w-np}]
+ * (np*m columns per k-point) under this wave's operators, Cholesky-QR and
+ * the Ritz eigenproblem (the reference orthonormalises by Householder and
+ * calls zheev), and E = basis * the lowest m Ritz vectors.  Ritz values at
+ * or below the null space (lambda <= 1e-7) are skipped; a k-point whose
+ * basis cannot supply m Ritz vectors falls back to its previous wave's
+ * eigenvectors. */
+static int extrapolate(mxg_solver *s)
+{
+  int np = s->have_prev < s->order ? s->have_prev : s->order, K = s->K, m = s->m, ns, k, j, q, bad = 0;
+  int pr[3];
+  const void *pp[3];
+  if(np <= 1) {
+    L_(mxk_convert(s->pe, s->Eprev[0], s->pe, s->E, elen(s, s->L), s->st));
+    return 0;
+  }
+  ns = np * m;
+  for(q = 0; q < np; q++) { pr[q] = s->pe; pp[q] = s->Eprev[q]; }
+  L_(mxk_block_gram(s->n[s->L], m, K, s->ph, kap(s, s->L), np, pr, pp, 0, 0, s->ga, s->gm, s->gscratch,
+                    s->gscratch_bytes, s->st));
+  s->launches++;
+  for(k = 0; k < K; k++)
+    for(j = 0; j < ns; j++) s->h_sel[k * ns + j] = 1;
+  TRY((int) cudaMemcpyAsync(s->sel, s->h_sel, sizeof(int) * ns * K, cudaMemcpyHostToDevice, s->st));
+  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop_tol(s), 1.0 + 1e-7, s->coef, s->theta, s->info,
+                       s->rwork, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < K; k++)
+    if(s->h_info[k] < m) bad = 1;
+  if(bad) {
+    L_(mxk_convert(s->pe, s->Eprev[0], s->pe, s->E, elen(s, s->L), s->st));
+    return 0;
+  }
+  L_(mxk_block_combine(s->n[s->L], m, K, np, pr, pp, s->coef, ns, 0, s->combw, s->pe, s->E, s->st));
+  return 0;
+}
+
 int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field *yf, double *lambda,
                     int *steps, double *res)
 {
   int w, k, i, m = s->m, K = s->K;
   float ms;
   double total = 0.0;
+  TRY((int) cudaSetDevice(s->device));
   s->launches = 0;
   s->restarts = 0;
   s->have_prev = 0;   /* every call starts cold; later waves of this call start warm */
@@ -708,10 +804,13 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
       if(s->timing) fprintf(stderr, "wave %d: cold start incl. finest-level steps %.3f s\n", w, now_s() - tc);
     }
     else {
-      /* warm start from the k-point one wave earlier (extrapolation 'n');
-       * its eigenvectors are divergence-free for their own Bloch phases,
-       * not for these, so they are lifted (and centred at Gamma) first */
-      L_(mxk_convert(s->pe, s->Eprev, s->pe, s->E, elen(s, s->L), s->st));
+      /* warm start from the same slot of the earlier waves
+       * (exp_bloch2d.c:814-895): with one stored wave, or extrapolation
+       * 'n', its eigenvectors; otherwise the lowest Ritz vectors of this
+       * k-point's operator in the span of the stored waves' blocks.  They
+       * are divergence-free for their own Bloch phases, not for these, so
+       * they are lifted (and centred at Gamma) first */
+      TRY(extrapolate(s));
       if(s->o.center) L_(mxk_center(s->n[s->L], m, s->K, s->gamma, s->pe, s->E, s->cacc, s->st));
       TRY(lift(s, s->L, s->pe, s->E));
       TRY(residual(s, s->L, 0));
@@ -741,8 +840,15 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
         if(res) res[(size_t) (k0 + k) * m + i] = s->h_res[k * m + i];
       }
     }
-    L_(mxk_convert(s->pe, s->E, s->pe, s->Eprev, elen(s, s->L), s->st));
-    s->have_prev = 1;
+    {
+      /* keep this wave's eigenvectors, the oldest stored wave gives way */
+      void *t = s->Eprev[s->order - 1];
+      int q;
+      for(q = s->order - 1; q > 0; q--) s->Eprev[q] = s->Eprev[q - 1];
+      s->Eprev[0] = t;
+      L_(mxk_convert(s->pe, s->E, s->pe, s->Eprev[0], elen(s, s->L), s->st));
+      if(s->have_prev < s->order) s->have_prev++;
+    }
     s->K_prev = K;
   }
   s->last_ms = total;
@@ -762,10 +868,11 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
  * k = (2 pi ix / (steps - 1) - pi, 2 pi iy / (steps - 1) - pi) for
  * ix, iy = 0 .. steps-1, solved in waves of the solver's K k-points taken in
  * row order (iy outer, ix inner).  Wave 0 starts cold; every later wave
- * starts from the eigenvectors of the wave before it, whose slot i holds the
- * k-point K positions earlier on the grid -- K / steps rows lower when K is a
- * multiple of steps -- and the first block step's Rayleigh-Ritz over
- * [E, X] plays the part of the reference's Rayleigh extrapolation.
+ * starts from the same slots of the waves before it (extrapolate), slot i
+ * holding the k-point K positions earlier on the grid -- K / steps rows
+ * lower when K is a multiple of steps, so that with K = steps every k-point
+ * is extrapolated from the same column of the rows below it, as the
+ * reference's yext extrapolation (exp_blochsurf.c:332-406, 1066-1489).
  * Outputs are indexed (iy * steps + ix) as in mxg_bloch_solve. */
 int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, double *residual)
 {
@@ -795,7 +902,8 @@ int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host)
   size_t k, v, e;
   unsigned char *buf = malloc(es * tot);
   double *h = (double *) host;
-  int err = (int) cudaMemcpy(buf, s->E, es * tot, cudaMemcpyDeviceToHost);
+  int err = (int) cudaSetDevice(s->device);
+  if(!err) err = (int) cudaMemcpy(buf, s->E, es * tot, cudaMemcpyDeviceToHost);
   for(k = 0; !err && k < (size_t) s->K; k++)
     for(v = 0; v < (size_t) s->m; v++)
       for(e = 0; e < per; e++) {
@@ -814,6 +922,11 @@ int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host)
   return err;
 }
 
+int mxg_solver_restarts(const mxg_solver *s)
+{
+  return s->restarts;
+}
+
 int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches)
 {
   if(ms) *ms = s->last_ms;
@@ -823,31 +936,33 @@ int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches)
 
 int mxg_solver_profile(mxg_solver *s, int enable)
 {
+  int q;
   if(enable && !s->pev) {
-    int q;
     s->maxpev = 4096;
-    s->pev = malloc(sizeof(cudaEvent_t) * s->maxpev);
+    s->pev = calloc(s->maxpev, sizeof(cudaEvent_t));
+    s->ptag = calloc(s->maxpev / 2, sizeof(int));
+    s->pbytes = calloc(s->maxpev / 2, sizeof(double));
+    if(!s->pev || !s->ptag || !s->pbytes) return MXG_ENOMEM;
     for(q = 0; q < s->maxpev; q++)
       if(cudaEventCreate(&s->pev[q])) return MXG_ENOMEM;
   }
   s->prof = enable;
   s->npev = 0;
-  s->prof_ms = 0.0;
-  s->prof_count = 0;
+  for(q = 0; q < MXG_KT_N; q++) {
+    s->prof_ms[q] = 0.0;
+    s->prof_bytes[q] = 0.0;
+    s->prof_count[q] = 0;
+  }
   return 0;
 }
 
-int mxg_solver_kernel_time(mxg_solver *s, double *ms, long *count, double *bytes_per_sweep)
+int mxg_solver_kernel_time(mxg_solver *s, int which, double *ms, long *count, double *bytes)
 {
-  /* algorithmic bytes of one forward or backward AFW sweep at the finest
-   * level (both row phases): read x, b and kappa once, write x once:
-   * 3 * 2n^2 complex entries per vector plus n^2 kappa values */
-  size_t n = (size_t) s->n[s->L];
+  if(which < 0 || which >= MXG_KT_N) return MXG_EINVAL;
   if(s->prof && s->npev) prof_flush(s);
-  if(ms) *ms = s->prof_ms;
-  if(count) *count = s->prof_count;
-  if(bytes_per_sweep)
-    *bytes_per_sweep = (double) s->K * s->m * 3.0 * 2.0 * n * n * mxk_elem_size(s->pg) + (double) n * n * 4.0;
+  if(ms) *ms = s->prof_ms[which];
+  if(count) *count = s->prof_count[which];
+  if(bytes) *bytes = s->prof_bytes[which];
   return 0;
 }
 

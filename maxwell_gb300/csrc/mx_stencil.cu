@@ -1490,6 +1490,14 @@ extern "C" int center_edge2d_gpu_noalloc(int n, int m, int K, const int* gamma_f
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int) e;
   if (dev < 0 || dev >= kMaxDevices) return MXG_EINVAL;
+  if (stream) {
+    // the scratch address below belongs to the current device: a stream of
+    // another device is a usage error, not a launch failure
+    int sdev = -1;
+    e = cudaStreamGetDevice((cudaStream_t) stream, &sdev);
+    if (e != cudaSuccess) return (int) e;
+    if (sdev != dev) return MXG_EINVAL;
+  }
   double* sums = g_center_ptr[dev].load();
   if (!sums) {
     // set-up of this device: the same address whoever gets here first

@@ -40,6 +40,9 @@ void om_prolong_edge(int nc, om_cplx xf, om_cplx yf, om_cplx alpha,
 void om_restrict_edge(int nc, om_cplx xf, om_cplx yf, om_cplx alpha,
                       const om_cplx *f, om_cplx *c);
 void om_center_edge(int n, om_cplx *x);
+void om_nullprod_edge(int n, const om_cplx *x, om_cplx *xprod, om_cplx *yprod);
+void om_nulladd_edge(int n, om_cplx xalpha, om_cplx yalpha, om_cplx *x);
+double om_normmax(long len, const om_cplx *x);
 void om_dense_edge(int n, const double *kappa, om_cplx xf, om_cplx yf,
                    om_cplx alpha, om_cplx beta, om_cplx *a);
 
@@ -57,11 +60,14 @@ void om_gradient(int n, om_cplx xf, om_cplx yf, om_cplx alpha,
 void om_adjgradient(int n, om_cplx xf, om_cplx yf, om_cplx alpha,
                     const om_cplx *e, om_cplx *v);
 void om_dense_node(int n, om_cplx xf, om_cplx yf, int fixnull, om_cplx *a);
+void om_center_node(int n, om_cplx *v);
 
 /* ---- grid (grid2d.c) ---- */
 void om_coarsen_kappa(int n, const double *kfine, double *kcoarse);
 void om_disc_kappa(int n, int ndiscs, const double *discs /* eps, cx, cy, r */,
                    double eps_base, double *kappa);
+void om_pattern_kappa(int n, int nrect, const double *rect, int ncirc, const double *circ,
+                      double eps_base, double *kappa);
 
 /* ---- dense linear algebra (linalg.c replacements) ---- */
 int om_potrf(int n, om_cplx *a);
@@ -104,6 +110,11 @@ int om_bloch_solve(const om_opts *o, const double *kappa_fine,
                    int nk, const om_cplx *xfs, const om_cplx *yfs,
                    double *lambda_out, int *steps_out, double *res_out,
                    om_cplx *evec_out);
+/* the same, with the wall-clock seconds spent on every k-point (may be NULL) */
+int om_bloch_solve_timed(const om_opts *o, const double *kappa_fine,
+                         int nk, const om_cplx *xfs, const om_cplx *yfs,
+                         double *lambda_out, int *steps_out, double *res_out,
+                         om_cplx *evec_out, double *seconds_out);
 
 /* Eigenvalue sensitivity with respect to the permittivity of every cell. */
 void om_eps_sensitivity(int n, const double *kappa, om_cplx xf, om_cplx yf,

@@ -63,7 +63,12 @@ class Oracle:
         L.om_massprod_edge.restype = _Cplx
         L.om_norm2.restype = D
         L.om_norm2.argtypes = [C.c_long, V]
+        L.om_normmax.restype = D
+        L.om_normmax.argtypes = [C.c_long, V]
+        L.om_dot.restype = _Cplx
+        L.om_dot.argtypes = [C.c_long, V, V]
         L.om_bloch_solve.restype = I
+        L.om_bloch_solve_timed.restype = I
         L.om_rr_svqb.restype = I
         L.om_potrf.restype = I
         L.om_heev.restype = I
@@ -113,6 +118,34 @@ class Oracle:
         x = _cvec(x).copy()
         self.lib.om_center_edge(C.c_int(n), _p(x))
         return x
+
+    def nullprod_edge(self, n, x):
+        xp, yp = _Cplx(), _Cplx()
+        self.lib.om_nullprod_edge(C.c_int(n), _p(_cvec(x)), C.byref(xp), C.byref(yp))
+        return complex(xp.re, xp.im), complex(yp.re, yp.im)
+
+    def nulladd_edge(self, n, xalpha, yalpha, x):
+        x = _cvec(x).copy()
+        self.lib.om_nulladd_edge(C.c_int(n), _cz(xalpha), _cz(yalpha), _p(x))
+        return x
+
+    def normmax(self, x):
+        x = _cvec(x)
+        return self.lib.om_normmax(C.c_long(x.size), _p(x))
+
+    def center_node(self, n, v):
+        v = _cvec(v).copy()
+        self.lib.om_center_node(C.c_int(n), _p(v))
+        return v
+
+    def dot(self, x, y):
+        x, y = _cvec(x), _cvec(y)
+        r = self.lib.om_dot(C.c_long(x.size), _p(x), _p(y))
+        return complex(r.re, r.im)
+
+    def norm2(self, x):
+        x = _cvec(x)
+        return self.lib.om_norm2(C.c_long(x.size), _p(x))
 
     def dense_edge(self, n, kappa, xf, yf, alpha, beta):
         a = np.zeros((2 * n * n) ** 2, np.complex128)
@@ -169,6 +202,14 @@ class Oracle:
         self.lib.om_disc_kappa(C.c_int(n), C.c_int(len(d) // 4), _p(d), C.c_double(eps_base), _p(k))
         return k
 
+    def pattern_kappa(self, n, rects, circles, eps_base=1.0):
+        r = np.ascontiguousarray(np.asarray(rects, np.float64).reshape(-1))
+        c = np.ascontiguousarray(np.asarray(circles, np.float64).reshape(-1))
+        k = np.zeros(n * n, np.float64)
+        self.lib.om_pattern_kappa(C.c_int(n), C.c_int(len(r) // 5), _p(r) if len(r) else None,
+                                  C.c_int(len(c) // 4), _p(c) if len(c) else None, C.c_double(eps_base), _p(k))
+        return k
+
     # ---- dense ----
     def heev(self, a):
         n = a.shape[0]
@@ -176,6 +217,15 @@ class Oracle:
         w = np.zeros(n)
         self.lib.om_heev(C.c_int(n), _p(a), _p(w))
         return w, a
+
+    def chol_solve(self, a, b):
+        """A^-1 b by the oracle's Cholesky factorisation (om_potrf, om_potrs)."""
+        n = a.shape[0]
+        f = np.asfortranarray(a, np.complex128).copy(order="F")
+        info = self.lib.om_potrf(C.c_int(n), _p(f))
+        x = _cvec(b).copy()
+        self.lib.om_potrs(C.c_int(n), _p(f), _p(x))
+        return info, x
 
     def hegv(self, a, b):
         n = a.shape[0]
@@ -220,7 +270,7 @@ class Oracle:
     def bloch_solve(self, kappa_fine, factors, *, n0, L, ieigs, m, method=0, max_nested=20,
                     max_steps=40, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1,
                     center=1, extrapolation="2", wave=1, relative=1, tol=1e-8,
-                    want_vectors=False):
+                    want_vectors=False, want_times=False):
         class Opts(C.Structure):
             _fields_ = [(f, C.c_int) for f in (
                 "n0", "L", "ieigs", "m", "method", "max_nested", "max_steps", "prec_steps",
@@ -237,9 +287,12 @@ class Oracle:
         res = np.zeros((nk, m))
         n = n0 << L
         ev = np.zeros((nk, m, 2 * n * n), np.complex128) if want_vectors else None
-        st = self.lib.om_bloch_solve(C.byref(o), _p(np.ascontiguousarray(kappa_fine, np.float64)),
-                                     C.c_int(nk), _p(xfs), _p(yfs), _p(lam), _p(steps), _p(res),
-                                     _p(ev) if ev is not None else None)
+        secs = np.zeros(nk)
+        st = self.lib.om_bloch_solve_timed(C.byref(o), _p(np.ascontiguousarray(kappa_fine, np.float64)),
+                                           C.c_int(nk), _p(xfs), _p(yfs), _p(lam), _p(steps), _p(res),
+                                           _p(ev) if ev is not None else None, _p(secs))
+        if want_times:
+            return st, lam, steps, res, ev, secs
         return st, lam, steps, res, ev
 
     def eps_sensitivity(self, n, kappa, xf, yf, vecs, weights):

@@ -40,6 +40,7 @@ def test_no_device_means_errors_not_results(built):
     o = mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8)
     s = mx.lib().mxg_solver_new(C.byref(o), np.ones(256).ctypes.data_as(C.c_void_p))
     assert not s
+    assert mx.lib().mxg_set_device(0) != 0   # no device to select
 
 
 def test_solver_rejects_bad_options(built):
@@ -47,7 +48,8 @@ def test_solver_rejects_bad_options(built):
            mx.SolveOpts(8, 1, 8, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8),    # ieigs > m
            mx.SolveOpts(8, 1, 4, 40, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8),   # m > 16
            mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 0, 1, 1e-8),    # wave 0
-           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8, 2)]  # no such smoother
+           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8, 2),  # no such smoother
+           mx.SolveOpts(8, 1, 4, 6, 1, 1, 5, 5, 2, 5, 2, 1, 1, 1, 1, 1e-8, 1, 0.0, ord("3"))]  # extrapolation
     for o in bad:
         assert not mx.lib().mxg_solver_new(C.byref(o), np.ones(256).ctypes.data_as(C.c_void_p))
 
@@ -83,13 +85,12 @@ def test_c_caller_links_every_declared_function(built):
     assert r.returncode == 0, r.stderr
 
 
-def test_integration_example_compiles():
-    """The C caller shown in INTEGRATION.md compiles against the header
-    without warnings."""
+def test_c_caller_example_compiles(built):
+    """tests/c_caller_example.c, a reference-style C caller of the solver,
+    compiles against the header without warnings and links against the
+    library."""
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    text = open(os.path.join(root, "INTEGRATION.md")).read()
-    start = text.index("```c\n") + len("```c\n")
-    src = text[start:text.index("```", start)]
-    r = subprocess.run(["gcc", "-x", "c", "-std=c11", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
-                        "-I", os.path.join(root, "include"), "-"], input=src, capture_output=True, text=True)
+    src = os.path.join(root, "tests", "c_caller_example.c")
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-c", src, "-o", os.devnull,
+                        "-I", os.path.join(root, "include")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -20,14 +20,15 @@ def _free_port():
 
 def _rank(rank, ws, port, out):
     import torch.distributed as dist
-    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
     sys.path.insert(0, ROOT)
     import bench
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     try:
         k = bench.rank_kpoints(ws, rank)
         t = bench.max_over_ranks([1.0 + rank, 10.0 - rank])
-        out.put((rank, k.tolist(), t))
+        out.put((rank, k.tolist(), t, bench.rank_device()))
     finally:
         dist.destroy_process_group()
 
@@ -48,11 +49,12 @@ def test_kpoint_partition_and_timing_reduction():
         p.join(timeout=60)
         assert p.exitcode == 0
     got.sort()
+    assert [d for _, _, _, d in got] == list(range(ws))             # rank r drives GPU r
     full = bench.gamma_x_m_gamma(bench.NK * ws)
-    parts = [np.array(k) for _, k, _ in got]
+    parts = [np.array(k) for _, k, _, _ in got]
     assert all(len(p) == bench.NK for p in parts)                 # fixed work per rank
     joined = np.concatenate(parts)
     order = np.lexsort(joined.T[::-1])
     assert np.allclose(joined[order], full[np.lexsort(full.T[::-1])])   # every point exactly once
-    for _, _, t in got:
+    for _, _, t, _ in got:
         assert t == [2.0, 10.0]                                     # max over ranks, element-wise

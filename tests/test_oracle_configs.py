@@ -1,0 +1,42 @@
+"""The oracle and the benchmark's inputs at the task's configurations (CPU).
+
+* The permittivity fixtures record the cell count inside the disc and the
+  sum of 1/eps; the oracle's rasterisation (setpattern_grid2d's rule) and
+  the benchmark's own (bench.disc_kappa) reproduce them exactly.
+* The oracle restatement's LOBPCG reproduces the reference's own block
+  PINVIT eigenvalues of config 1 (64^2, tests/golden/config1_n64_disc.npz)
+  at two k-points to 1e-8 relative.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+@pytest.mark.parametrize("name", ["config1_n64_disc.npz", "headline_n512_disc.npz"])
+def test_fixture_permittivity(oracle, golden, name):
+    g = golden(name)
+    n = int(g["n0"]) << int(g["L"])
+    kap = oracle.disc_kappa(n, [g["disc"]], float(g["eps_base"]))
+    assert int((kap < 1.0).sum()) == int(g["inside"])
+    assert kap.sum() == pytest.approx(float(g["kappa_sum"]), rel=1e-15)
+    if name.startswith("headline"):
+        import bench
+        assert np.array_equal(bench.disc_kappa(n), kap)
+
+
+def test_oracle_matches_config1_reference(oracle, golden):
+    g = golden("config1_n64_disc.npz")
+    n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
+    kap = oracle.disc_kappa(n0 << L, [g["disc"]], float(g["eps_base"]))
+    pick = [3, 11]
+    st, lam, steps, res, _ = oracle.bloch_solve(kap, g["factors"][pick], n0=n0, L=L, ieigs=ie, m=m, method=1,
+                                                max_nested=40, max_steps=80, tol=1e-10, relative=1,
+                                                extrapolation="n", wave=1)
+    assert st == 0
+    want = g["lam"][pick, :ie]
+    assert (np.abs(lam[:, :ie] - want) / want).max() < 1e-8
