@@ -422,12 +422,61 @@ def run_kernels(args):
                           "frac": gbs / hbm}), flush=True)
 
 
+def checkerboard_kappa(n: int, blocks: int = 16, seed: int = 0) -> np.ndarray:
+    """1/eps per cell of a seeded random blocks x blocks checkerboard with eps
+    drawn from {1, 4, 8.9, 12}, in the order i + j n."""
+    rng = np.random.default_rng(seed)
+    eps = rng.choice([1.0, 4.0, 8.9, 12.0], size=(blocks, blocks))
+    return np.ascontiguousarray((1.0 / np.kron(eps, np.ones((n // blocks, n // blocks)))).reshape(-1))
+
+
+def run_config5(args):
+    """The large-mesh configuration: 2048^2 cells (8,388,608 edges), a seeded
+    16 x 16 checkerboard of eps in {1, 4, 8.9, 12}, 8 k-points at the
+    high-symmetry corners and edge midpoints (Gamma, X, Y, M, the midpoints of
+    Gamma-X, Gamma-Y, Gamma-M and X-M), 24 pairs with block 32 via LOBPCG,
+    9 multigrid levels 2048 .. 8 in FP32 complex, relative residual 1e-9,
+    then one refinement sweep and the FP64 residual check.  Solved in two
+    batches of 4 k-points (about 120 GB on the device each).  Not the
+    headline metric: one JSON line."""
+    import maxwell_gb300 as mx
+    mx.check(mx.lib().mxg_set_device(rank_device()), "mxg_set_device")
+    n0, L, ie, m, tol = 8, 8, 24, 32, 1e-9
+    n = n0 << L
+    kap = checkerboard_kappa(n)
+    pi = np.pi
+    kpts = np.array([(0, 0), (pi, 0), (0, pi), (pi, pi), (pi / 2, 0), (0, pi / 2), (pi / 2, pi / 2), (pi, pi / 2)])
+    fac = factors_of(kpts)
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, max_nested=MAX_NESTED, max_steps=120,
+                  wave=4, relative=1, tol=tol, refine=1)
+    ms_all, lams, steps_all, res_max, fp_max, launches = 0.0, [], [], 0.0, 0.0, 0
+    for b in range(2):
+        lam, st, res = s.solve(fac[4 * b:4 * b + 4])
+        ms, nl = s.stats()
+        ms_all += ms
+        launches += nl
+        fp = s.check_fp64()
+        lams.append(lam[:, :ie]); steps_all += st.tolist()
+        res_max = max(res_max, float(res[:, :ie].max()))
+        fp_max = max(fp_max, float(fp[:, :ie].max()))
+    print(json.dumps({"metric": "k-points/s, 2048^2 checkerboard, 24 pairs block 32, relative residual 1e-9",
+                      "value": len(kpts) / (ms_all / 1e3), "unit": "k-points/s", "seconds": ms_all / 1e3,
+                      "steps_per_k": steps_all, "max_rel_residual": res_max, "max_rel_residual_fp64": fp_max,
+                      "gpu_launches": launches, "lambda_first": [float(v) for v in np.concatenate(lams)[:, 0]],
+                      "config": {"workload": "2048^2, 16x16 checkerboard eps {1,4,8.9,12} seed 0, 8 k-points "
+                                             "(Gamma X Y M and midpoints), 24 pairs block 32, LOBPCG, 9 levels, "
+                                             "relative residual 1e-9 + refinement sweep + FP64 check",
+                                 "batches": "2 x 4 k-points"}}), flush=True)
+
+
 def run_surface(args):
     """The full-zone surface (exp_blochsurf): 256^2 cells, four discs eps = 10
     of radius 0.15 centred at (0.25|0.75, 0.25|0.75), a 32 x 32 k-grid over
-    [-pi, pi]^2 solved in waves of 64 (each wave starting from the previous
-    one), 12 pairs with block 16 via LOBPCG, mixed precision, relative
-    residual 1e-8.  Not the headline metric: one JSON line of k-points/s."""
+    [-pi, pi]^2 solved in waves of 64 (two rows; every wave after the first
+    starts from the Rayleigh-Ritz extrapolation over the same slots of the
+    three waves before it), 12 pairs with block 16 via LOBPCG, mixed
+    precision, relative residual 1e-8.  Not the headline metric: one JSON
+    line of k-points/s."""
     import maxwell_gb300 as mx
     n0, L, steps, wave = 8, 5, 32, 64
     n = n0 << L
@@ -440,7 +489,7 @@ def run_surface(args):
             inside |= (X - cx) ** 2 + (Y - cy) ** 2 <= 0.15 ** 2
     kap = np.ascontiguousarray(np.where(inside, 1.0 / 10.0, 1.0).reshape(-1))
     s = mx.Solver(kap, n0=n0, L=L, ieigs=IEIGS, m=BLOCK, method=1, precision=1, max_nested=MAX_NESTED,
-                  max_steps=60, wave=wave, relative=1, tol=TOL)
+                  max_steps=60, wave=wave, relative=1, tol=TOL, extrapolation="2")
     for _ in range(args.warmup):
         s.solve(factors_of(gamma_x_m_gamma(wave)))
     t0 = time.time()
@@ -452,6 +501,7 @@ def run_surface(args):
                       "steps_first_wave": float(st.reshape(-1)[:wave].mean()),
                       "steps_later_waves": float(st.reshape(-1)[wave:].mean()),
                       "max_rel_residual": float(res[..., :IEIGS].max()), "gpu_launches": nl,
+                      "cold_restarts": s.restarts(),
                       "config": {"workload": "256^2, 4 discs eps=10 r=0.15, 32x32 k-grid over the zone, "
                                              "waves of 64, 12 pairs block 16, LOBPCG, relative residual 1e-8"}}),
           flush=True)
@@ -468,11 +518,14 @@ def main():
     ap.add_argument("--nk", type=int, default=NK, help="k-points of the --kernels table")
     ap.add_argument("--reps", type=int, default=5, help="timed calls per kernel of the --kernels table")
     ap.add_argument("--surface", action="store_true", help="the full-zone surface workload instead of the metric")
+    ap.add_argument("--config5", action="store_true", help="the 2048^2 block-32 workload instead of the metric")
     args = ap.parse_args()
     if args.kernels:
         run_kernels(args)
     elif args.surface:
         run_surface(args)
+    elif args.config5:
+        run_config5(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

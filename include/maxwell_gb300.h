@@ -245,7 +245,7 @@ int pinvit_edge2d_gpu(int l, int smoother_steps, int prec_steps, int gradient_st
 /* ---------- the per-k eigensolver (exp_bloch2d.c:556-1053) ---------- */
 typedef struct {
   int n0, L;             /* coarse intervals, refinement levels (n = n0 << L) */
-  int ieigs, m;          /* wanted pairs, block size */
+  int ieigs, m;          /* wanted pairs, block size (m <= 32) */
   int method;            /* 0 block PINVIT + Ritz (exp_bloch2d), 1 LOBPCG */
   int precision;         /* 0 plain FP64, 1 mixed (FP32 multigrid, float-float eigenvectors) */
   int max_nested;        /* block steps per level of the nested iteration */
@@ -265,6 +265,9 @@ typedef struct {
                           * earlier waves (exp_bloch2d.c:814-895, maxwell_extra):
                           * 'n' or 0 their eigenvectors, '1' Rayleigh-Ritz over the last
                           * two waves, '2' over the last three */
+  int refine;            /* 1: after the finest level converges, one more block step with
+                          * every search column in the Ritz basis (the refinement sweep
+                          * of the 2048^2 configuration), residuals recomputed after it */
 } mxg_solve_opts;
 
 typedef struct mxg_solver mxg_solver;
@@ -295,6 +298,11 @@ int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of
  * kernel launches it issued */
 int mxg_solver_stats(const mxg_solver *s, double *ms, long *launches);
+/* The relative residuals ||(A+M) e - mu M e|| / (mu ||M e||) of the last
+ * solved wave (o.wave k-points x m vectors) recomputed in FP64: the
+ * eigenvectors converted to complex128 on the device and the residual
+ * formed by the complex128 operator kernel in double arithmetic. */
+int mxg_solver_check_fp64(mxg_solver *s, double *res);
 /* warm-started waves of the last mxg_bloch_solve / mxg_bloch_surface that
  * missed the tolerance and were solved again from a cold start */
 int mxg_solver_restarts(const mxg_solver *s);

@@ -38,7 +38,8 @@ class SolveOpts(C.Structure):
         "gradient_steps", "smoother_steps", "lift_e", "center", "wave", "relative")] + [("tol", C.c_double),
                                                                                   ("smoother", C.c_int),
                                                                                   ("drop", C.c_double),
-                                                                                  ("extrapolation", C.c_int)]
+                                                                                  ("extrapolation", C.c_int),
+                                                                                  ("refine", C.c_int)]
 
 
 class EpsPattern(C.Structure):
@@ -116,6 +117,7 @@ def lib() -> C.CDLL:
             "mxg_device_ok": (I, []),
             "mxg_set_device": (I, [I]),
             "mxg_solver_restarts": (I, [P]),
+            "mxg_solver_check_fp64": (I, [P, P]),
             "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
             "swap_edge2d_gpu": (I, [P, P]),
@@ -322,10 +324,10 @@ class Solver:
 
     def __init__(self, kappa_fine, *, n0, L, ieigs, m, method=1, precision=1, max_nested=20,
                  max_steps=60, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1, center=1,
-                 wave=1, relative=1, tol=1e-8, smoother=1, drop=0.0, extrapolation="n"):
+                 wave=1, relative=1, tol=1e-8, smoother=1, drop=0.0, extrapolation="n", refine=0):
         self.o = SolveOpts(n0, L, ieigs, m, method, precision, max_nested, max_steps, prec_steps,
                            gradient_steps, smoother_steps, lift_e, center, wave, relative, tol, smoother, drop,
-                           ord(extrapolation))
+                           ord(extrapolation), refine)
         self.n = n0 << L
         self.m, self.wave = m, wave
         k = np.ascontiguousarray(kappa_fine, np.float64)
@@ -364,6 +366,12 @@ class Solver:
         ms, launches = C.c_double(0), C.c_long(0)
         lib().mxg_solver_stats(self.h, C.byref(ms), C.byref(launches))
         return ms.value, launches.value
+
+    def check_fp64(self) -> np.ndarray:
+        """Relative residuals of the last wave recomputed in FP64 (wave, m)."""
+        r = np.zeros(self.wave * self.m)
+        check(lib().mxg_solver_check_fp64(self.h, _ptr(r)), "mxg_solver_check_fp64")
+        return r.reshape(self.wave, self.m)
 
     def restarts(self) -> int:
         """Warm-started waves of the last solve that were solved again cold."""

@@ -210,7 +210,7 @@ __device__ __forceinline__ cx<float> ld_any_f(int prec, const void* base, size_t
 // HI = dd for the mixed solver (column block 0 is cdd, the other blocks c64),
 // double for the plain solver (every block c128, every column high).
 template <typename HI>
-__global__ void k_block_gram(GramArgs a, int mh) {
+__global__ void k_block_gram(GramArgs a, int mh, int ebase) {
   int k = blockIdx.y, chunk = blockIdx.x;
   int n = a.n, m = a.m, ns = a.ns;
   int nent = ns * (ns + 1) / 2;
@@ -225,14 +225,16 @@ __global__ void k_block_gram(GramArgs a, int mh) {
   bool use_r = a.resid != nullptr;
   Seam<float> sf = seam_load<float>(a.ph, a.K, k, n);
   Seam<HI> sh = seam_load<HI>(a.ph, a.K, k, n);
-  constexpr int MAXE = 5;   // ns <= 48 -> nent <= 1176 <= 5*256
+  // a launch accumulates the entries [ebase, ebase + MAXE*GT) of the lower
+  // triangle (ns <= 48: one launch; larger blocks take several)
+  constexpr int MAXE = 5;
   cx<float> acc_a[MAXE], acc_m[MAXE];
   cx<HI> hacc_a[MAXE], hacc_m[MAXE];
   int ei[MAXE], ej[MAXE];
   for (int t = 0; t < MAXE; t++) {
     acc_a[t] = czero<float>(); acc_m[t] = czero<float>();
     hacc_a[t] = czero<HI>(); hacc_m[t] = czero<HI>();
-    int e = threadIdx.x + t * GT;
+    int e = ebase + threadIdx.x + t * GT;
     ei[t] = -1; ej[t] = -1;
     if (e < nent) {
       // row-major lower triangle: e = i(i+1)/2 + j, j <= i
@@ -351,7 +353,7 @@ __global__ void k_block_gram(GramArgs a, int mh) {
   double axy = (double) n * (double) n;
   double* out = a.partial + (((size_t) k * a.chunks + chunk) * nent) * 4;
   for (int t = 0; t < MAXE; t++) {
-    int e = threadIdx.x + t * GT;
+    int e = ebase + threadIdx.x + t * GT;
     if (e >= nent) continue;
     double ar = Real<HI>::to_double(hacc_a[t].re) + (double) acc_a[t].re;
     double ai = Real<HI>::to_double(hacc_a[t].im) + (double) acc_a[t].im;
@@ -947,7 +949,7 @@ static int gram_chunks(int K, size_t nsite) {
 extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa kap, int nb, const int* precs,
                               const void* const* ptrs, const void* resid, const double* theta, double* ga,
                               double* gm, double* scratch, size_t scratch_bytes, mx_stream s) {
-  if (nb < 1 || nb > 4 || nb * m > 48) return (int) cudaErrorInvalidValue;
+  if (nb < 1 || nb > 4 || nb * m > 96) return (int) cudaErrorInvalidValue;
   GramArgs a;
   a.n = n; a.m = m; a.K = K; a.nb = nb; a.ns = nb * m;
   for (int b = 0; b < 4; b++) {
@@ -985,10 +987,10 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
     k_block_gram_mixed<<<g, G2T, sm, st>>>(a);
   } else if (hi_dd) {
     cudaFuncSetAttribute(k_block_gram<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    k_block_gram<dd><<<g, GT, smem, st>>>(a, mh);
+    for (int eb = 0; eb < nent; eb += 5 * GT) k_block_gram<dd><<<g, GT, smem, st>>>(a, mh, eb);
   } else {
     cudaFuncSetAttribute(k_block_gram<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-    k_block_gram<double><<<g, GT, smem, st>>>(a, mh);
+    for (int eb = 0; eb < nent; eb += 5 * GT) k_block_gram<double><<<g, GT, smem, st>>>(a, mh, eb);
   }
   MX_CHECK_LAUNCH();
   size_t work = (size_t) nent * K;
@@ -1039,15 +1041,25 @@ extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, 
     MX_CHECK_LAUNCH();
     return 0;
   }
+  if (m > 256) return (int) cudaErrorInvalidValue;
   unsigned rows = 256 / m;
   dim3 g((unsigned) ((2 * (size_t) n * n + rows - 1) / rows), K), b(m, rows);
   size_t ncoef = (size_t) nb * m * m;
-  if (pout == MX_CDD)
-    k_block_combine<cdd, dd><<<g, b, ncoef * (sizeof(cx<dd>) + sizeof(cx<float>)), st>>>(a, (cdd*) out);
-  else if (pout == MX_C128)
-    k_block_combine<double2, double><<<g, b, ncoef * (sizeof(cx<double>) + sizeof(cx<float>)), st>>>(a, (double2*) out);
-  else
-    k_block_combine<float2, float><<<g, b, ncoef * (sizeof(cx<float>) * 2), st>>>(a, (float2*) out);
+  // the coefficients staged per block exceed the default 48 KB for blocks
+  // of more than about 24 vectors
+  if (pout == MX_CDD) {
+    size_t sm = ncoef * (sizeof(cx<dd>) + sizeof(cx<float>));
+    cudaFuncSetAttribute(k_block_combine<cdd, dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    k_block_combine<cdd, dd><<<g, b, sm, st>>>(a, (cdd*) out);
+  } else if (pout == MX_C128) {
+    size_t sm = ncoef * (sizeof(cx<double>) + sizeof(cx<float>));
+    cudaFuncSetAttribute(k_block_combine<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    k_block_combine<double2, double><<<g, b, sm, st>>>(a, (double2*) out);
+  } else {
+    size_t sm = ncoef * (sizeof(cx<float>) * 2);
+    cudaFuncSetAttribute(k_block_combine<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    k_block_combine<float2, float><<<g, b, sm, st>>>(a, (float2*) out);
+  }
   MX_CHECK_LAUNCH();
   return 0;
 }

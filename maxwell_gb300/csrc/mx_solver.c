@@ -96,6 +96,7 @@ struct mxg_solver {
   int restarts;                       /* warm-started waves solved again cold */
   int debug;                          /* per-step residual trace on stderr */
   int order;                          /* earlier waves a warm start combines (1, 2 or 3) */
+  int all_columns;                    /* Ritz basis with every search column (refinement) */
   int device;                         /* the CUDA device the solver lives on */
 };
 
@@ -159,7 +160,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   int l, K, m, ns, N0e, N0n;
   size_t es_g, es_e;
   double *kk[MAXL];
-  if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 16
+  if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 32
      || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 1
      || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'))
     return 0;
@@ -558,7 +559,7 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
   for(k = 0; k < K; k++)
     for(j = 0; j < nb; j++)
       for(i = 0; i < m; i++)
-        s->h_sel[k * ns + j * m + i] = j == 0 || !(s->h_res[k * m + i] <= s->o.tol);
+        s->h_sel[k * ns + j * m + i] = j == 0 || s->all_columns || !(s->h_res[k * m + i] <= s->o.tol);
   TRY((int) cudaMemcpyAsync(s->sel, s->h_sel, sizeof(int) * ns * K, cudaMemcpyHostToDevice, s->st));
   if(tm) cudaEventRecord(s->tev[PH_RR], s->st);
   L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop, theta_min, s->coef, s->theta, s->info, s->rwork,
@@ -670,6 +671,14 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
   }
   for(k = 0; k < K_active; k++)
     if(!converged_k(s, k)) s->h_steps[k] = maxsteps;
+  if(l == s->L && s->o.refine) {
+    /* the refinement sweep: one more block step with every column of the
+     * search blocks in the Ritz basis, then the residuals again */
+    s->all_columns = 1;
+    TRY(block_step(s, l, &have_p));
+    s->all_columns = 0;
+    TRY(residual(s, l, 1));
+  }
   return 0;
 }
 
@@ -920,6 +929,30 @@ int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host)
       }
   free(buf);
   return err;
+}
+
+/* Relative residuals of the last solved wave recomputed in FP64: the
+ * eigenvector block converted to complex128 (into the spare block En, of
+ * the same size), then the residual statistics of the complex128 kernel --
+ * (A+M) e, M e and r = (A+M) e - mu M e in double arithmetic -- with mu the
+ * returned eigenvalues + 1 (the final Rayleigh quotients). */
+int mxg_solver_check_fp64(mxg_solver *s, double *res)
+{
+  int k, i, m = s->m, K = s->K, l = s->L;
+  TRY((int) cudaSetDevice(s->device));
+  L_(mxk_convert(s->pe, s->E, MX_C128, s->En, elen(s, l), s->st));
+  TRY((int) cudaMemcpyAsync(s->mu, s->h_rq, sizeof(double) * m * K, cudaMemcpyHostToDevice, s->st));
+  TRY((int) cudaMemsetAsync(s->stats, 0, sizeof(double) * NSTAT * m * K, s->st));
+  L_(mxk_block_residual(s->n[l], m, K, s->ph, kap(s, l), s->mu, MX_C128, s->En, MX_C128, 0, s->stats, s->st));
+  TRY((int) cudaMemcpyAsync(s->h_stats, s->stats, sizeof(double) * NSTAT * m * K, cudaMemcpyDeviceToHost, s->st));
+  TRY((int) cudaStreamSynchronize(s->st));
+  for(k = 0; k < K; k++)
+    for(i = 0; i < m; i++) {
+      const double *st = s->h_stats + ((size_t) k * m + i) * NSTAT;
+      double mu = s->h_rq[k * m + i];
+      res[k * m + i] = sqrt(st[0] > 0.0 ? st[0] : 0.0) / (fabs(mu) * sqrt(st[1]) + 1e-300);
+    }
+  return upload_mu(s);
 }
 
 int mxg_solver_restarts(const mxg_solver *s)

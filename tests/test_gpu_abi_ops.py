@@ -140,9 +140,10 @@ def test_gram_and_lincomb(oracle, setup, prec):
     for k in range(K):
         for i in range(m):
             for j in range(m):
-                # entry (i, j) = u_i^H K u_j = energyprod_edge2d(u_j, u_i) (edge2d.c:1958)
-                wa = oracle.energyprod_edge(n, kap, *FACTORS[k], 1.0, 1.0, x[k, j], x[k, i])
-                wm = oracle.massprod_edge(n, *FACTORS[k], x[k, j], x[k, i])
+                # entry (i, j) = u_i^H K u_j = energyprod_edge2d(u_i, u_j), which
+                # returns CONJ(sum conj(u_j) (K u_i)) (edge2d.c:1958)
+                wa = oracle.energyprod_edge(n, kap, *FACTORS[k], 1.0, 1.0, x[k, i], x[k, j])
+                wm = oracle.massprod_edge(n, *FACTORS[k], x[k, i], x[k, j])
                 assert abs(A[k, i, j] - wa) < 1e-11 * abs(A[k]).max()
                 assert abs(M[k, i, j] - wm) < 1e-11 * abs(M[k]).max()
     coef = cv(rng, K, m, m)                      # coef[k][i][j]
@@ -168,9 +169,10 @@ def test_orthonormalize(oracle, setup, prec):
     assert not info.any()
     q = ex.get()
     for k in range(K):
-        G = np.array([[oracle.massprod_edge(n, *FACTORS[k], q[k, j], q[k, i]) for j in range(m)] for i in range(m)])
+        # massprod_edge(a, b) = a^H M b
+        G = np.array([[oracle.massprod_edge(n, *FACTORS[k], q[k, i], q[k, j]) for j in range(m)] for i in range(m)])
         assert np.abs(G - np.eye(m)).max() < 1e-11
-        R = np.array([[oracle.massprod_edge(n, *FACTORS[k], x[k, j], q[k, i]) for j in range(m)] for i in range(m)])
+        R = np.array([[oracle.massprod_edge(n, *FACTORS[k], q[k, i], x[k, j]) for j in range(m)] for i in range(m)])
         assert np.abs(np.tril(R, -1)).max() < 1e-11 * np.abs(R).max()
         assert (np.diag(R).real > 0).all() and np.abs(np.diag(R).imag).max() < 1e-11 * np.abs(R).max()
         assert rel(np.einsum("ij,ie->je", R, q[k]), x[k]) < 1e-12

@@ -70,8 +70,9 @@ def test_headline_config_matches_cpu_fp64(oracle, golden):
 def test_extrapolated_waves_match_oracle(oracle, extrapolation):
     """Eight k-points from Gamma towards X in waves of two: every wave after
     the first starts from the Ritz extrapolation over the earlier waves, as
-    the oracle's flow does k-point by k-point.  The warm waves converge
-    without a cold restart and in fewer steps than the cold wave."""
+    the oracle's flow does k-point by k-point (the second wave, with one
+    earlier wave stored, copies it).  The warm waves converge without a cold
+    restart, and the extrapolated ones in fewer steps than the cold wave."""
     n0, L, ie, m = 8, 2, 8, 12
     n = n0 << L
     kap = oracle.disc_kappa(n, [[8.9, 0.5, 0.5, 0.2]], 1.0)
@@ -82,9 +83,40 @@ def test_extrapolated_waves_match_oracle(oracle, extrapolation):
     lam, steps, res = s.solve(fac)
     assert res[:, :ie].max() <= 1e-9
     assert s.restarts() == 0
-    assert steps[2:].max() < steps[:2].max(), steps
+    assert steps[4:].max() < steps[:2].max(), steps
     st, lam_o, steps_o, res_o, _ = oracle.bloch_solve(kap, fac, n0=n0, L=L, ieigs=ie, m=m, method=1,
                                                       max_nested=40, max_steps=60, tol=1e-9, relative=1,
                                                       extrapolation=extrapolation, wave=1)
+    assert st == 0
+    assert (np.abs(lam[:, :ie] - lam_o[:, :ie]) / lam_o[:, :ie]).max() < 1e-8
+
+
+def checkerboard_kappa(n, blocks, seed):
+    """A seeded random checkerboard of blocks x blocks squares with eps drawn
+    from {1, 4, 8.9, 12} (the 2048^2 configuration's pattern at a smaller
+    size), 1/eps per cell in the order i + j n."""
+    rng = np.random.default_rng(seed)
+    eps = rng.choice([1.0, 4.0, 8.9, 12.0], size=(blocks, blocks))
+    return np.ascontiguousarray((1.0 / np.kron(eps, np.ones((n // blocks, n // blocks)))).reshape(-1))
+
+
+@pytest.mark.parametrize("m, ie", [(24, 18), (32, 24)])
+def test_large_block_matches_oracle(oracle, m, ie):
+    """Blocks above 16 (the 2048^2 configuration's block 32 with 24 pairs):
+    the Gram matrices of [E X P] (up to 96 columns) in several entry passes,
+    the generic combination, the refinement sweep and the in-library FP64
+    residual check, against the oracle's complex128 solve at 1e-8."""
+    n0, L = 8, 2
+    n = n0 << L
+    kap = checkerboard_kappa(n, 4, 5)
+    fac = np.exp(1j * np.array([[np.pi / 2, 0.0], [np.pi, np.pi]]))
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, max_nested=40, max_steps=80, wave=2,
+                  relative=1, tol=1e-9, refine=1)
+    lam, steps, res = s.solve(fac)
+    assert res[:, :ie].max() <= 1e-9, steps
+    fp = s.check_fp64()
+    assert fp[:, :ie].max() <= 1.01e-9
+    st, lam_o, _, _, _ = oracle.bloch_solve(kap, fac, n0=n0, L=L, ieigs=ie, m=m, method=1, max_nested=40,
+                                            max_steps=80, tol=1e-10, relative=1, extrapolation="n", wave=1)
     assert st == 0
     assert (np.abs(lam[:, :ie] - lam_o[:, :ie]) / lam_o[:, :ie]).max() < 1e-8
