@@ -156,12 +156,25 @@ int gssymm_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge
  * one parallel pass; dir 0 forward, 1 backward (reverse colour order), 2 both.
  * The solver's default smoother (mxg_solve_opts.smoother = 1). */
 int gscolour_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x, int dir);
+/* point Gauss-Seidel, edge by edge, in the reference's interleaved row order
+ * (gsforward/gsbackward/gssymm_simple_edge2d, edge2d.c:3890-5581): the
+ * smoother of the Hiptmair cycle */
+int gsforward_simple_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+int gsbackward_simple_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
+int gssymm_simple_edge2d_gpu(mxg_field alpha, mxg_field beta, const edge2d_gpu *b, edge2d_gpu *x);
 /* transfers (edge2d.c:5583-5705) */
 int prolongation_edge2d_gpu(mxg_field alpha, const edge2d_gpu *c, edge2d_gpu *f);
 int restriction_edge2d_gpu(mxg_field alpha, const edge2d_gpu *f, edge2d_gpu *c);
 /* vcycle_edge2d (edge2d.c:5707-5754): b, x, d arrays of L+1 levels */
 int vcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2d_gpu **x,
                       edge2d_gpu **d);
+/* hcycle_edge2d (edge2d.c:5756-5823): the Hiptmair cycle for A+M -- point
+ * Gauss-Seidel plus a correction in the gradients (nu node Gauss-Seidel
+ * sweeps on G^H of the residual) on every level, the coarse dense solve
+ * with Ac (or nu symmetric point sweeps); bg, xg: node work vectors of the
+ * L+1 levels */
+int hcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2d_gpu **x, edge2d_gpu **d,
+                      node2d_gpu **bg, node2d_gpu **xg);
 /* densematrix_edge2d (edge2d.c:5870-6116) for every k of the grid */
 int densematrix_edge2d_gpu(mxg_field alpha, mxg_field beta, const grid2d_gpu *gr, matrix_gpu *a);
 /* host <-> device in the reference's dense order (denseto/densefrom_edge2d) */
@@ -258,7 +271,8 @@ typedef struct {
   int wave;              /* k-points per batch; batch w starts from batch w-1 */
   int relative;          /* stopping rule: 0 absolute defect, 1 relative residual */
   double tol;
-  int smoother;          /* edge smoother: 0 the reference's row order, 1 four colours */
+  int smoother;          /* preconditioner: AFW V-cycle with 0 the reference's row order or
+                          * 1 four colours; 2 the Hiptmair cycle (hcycle_edge2d) */
   double drop;           /* Ritz step: columns whose Cholesky-QR pivot^2 falls below this
                           * are dropped; 0 = 1e-6 (mixed) or 1e-12 (plain FP64) */
   int extrapolation;     /* start of every wave after the first, from the same slots of
@@ -293,6 +307,28 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xfactor, const mxg_f
  * reference's extrapolation along y).  Outputs as mxg_bloch_solve, indexed
  * (iy * steps + ix). */
 int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, double *residual);
+/* Eigenvector continuity and Chern partial sums along the k-points of the
+ * last mxg_bloch_solve (exp_bloch2d.c:1058-1216), which must have fitted one
+ * wave (nk <= o.wave), taken as consecutive points of a curve.  For every
+ * point l >= 1, with eold0 / eold1 the adjusted vectors of points l-1 / l-2
+ * and the mass products taken with M(k_l):
+ *   continuity 'r': for i < ieigs, the vector closest to eold0_i (after a
+ *     vertex, vertex[l-1] != 0) or to 2 eold0_i - eold1_i takes place i
+ *     (swapping eigenvalues; sign[l] counts the swaps so far), then 's';
+ *   continuity 's': every vector is scaled by a unit phase that makes
+ *     e_i^H M eold0_i (after a vertex) or e_i^H M (2 eold0_i - eold1_i)
+ *     real and positive; 'n' leaves the vectors as they are;
+ *   Chern sums, for i < chern_vectors: += (i/2) eold0_i^H M (e_i - eold0_i)
+ *     after a vertex, else (i/2) eold0_i^H M (e_i - eold1_i), plus
+ *     (i/2) e_i^H M (e_i - eold0_i) when point l is itself a vertex.
+ * vertex: nk flags (the curve's corners; the first point counts as one,
+ * as exp_bloch2d.c:447 starts); lambda: the nk*m eigenvalues of the solve,
+ * reordered in place; chern: nk*chern_vectors partial sums (row 0 zero);
+ * sign: nk swap counts or NULL.  The solver's eigenvectors are left
+ * adjusted (mxg_solver_eigenvectors returns them so).  Mass products in
+ * complex128 on the device; the decisions on the host. */
+int mxg_bloch_continuity(mxg_solver *s, int nk, const int *vertex, int continuity, int chern_vectors,
+                         double *lambda, mxg_field *chern, int *sign);
 /* eigenvectors of the last solved batch: wave k-points x m vectors in dense order */
 int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of

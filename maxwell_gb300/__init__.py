@@ -118,6 +118,11 @@ def lib() -> C.CDLL:
             "mxg_set_device": (I, [I]),
             "mxg_solver_restarts": (I, [P]),
             "mxg_solver_check_fp64": (I, [P, P]),
+            "mxg_bloch_continuity": (I, [P, I, P, I, I, P, P, P]),
+            "gsforward_simple_edge2d_gpu": (I, [Field, Field, P, P]),
+            "gsbackward_simple_edge2d_gpu": (I, [Field, Field, P, P]),
+            "gssymm_simple_edge2d_gpu": (I, [Field, Field, P, P]),
+            "hcycle_edge2d_gpu": (I, [I, I, P, P, P, P, P, P]),
             "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
             "swap_edge2d_gpu": (I, [P, P]),
@@ -366,6 +371,19 @@ class Solver:
         ms, launches = C.c_double(0), C.c_long(0)
         lib().mxg_solver_stats(self.h, C.byref(ms), C.byref(launches))
         return ms.value, launches.value
+
+    def continuity(self, lam, vertex, continuity="s", chern_vectors=0):
+        """mxg_bloch_continuity on the last solve: returns the reordered
+        eigenvalues, the Chern partial sums (nk, chern_vectors) and the swap
+        counts (nk)."""
+        lam = np.ascontiguousarray(np.array(lam, np.float64))
+        nk = lam.shape[0]
+        v = np.ascontiguousarray(np.asarray(vertex, np.int32))
+        ch = np.zeros((nk, max(chern_vectors, 1)), np.complex128)
+        sg = np.zeros(nk, np.int32)
+        check(lib().mxg_bloch_continuity(self.h, nk, _ptr(v), ord(continuity), chern_vectors, _ptr(lam), _ptr(ch),
+                                          _ptr(sg)), "mxg_bloch_continuity")
+        return lam, ch[:, :chern_vectors], sg
 
     def check_fp64(self) -> np.ndarray:
         """Relative residuals of the last wave recomputed in FP64 (wave, m)."""

@@ -409,6 +409,26 @@ int gscolour_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_g
                             g->st);
 }
 
+static int gs_simple(double a, double b, const edge2d_gpu *bb, edge2d_gpu *x, int dir)
+{
+  const grid2d_gpu *g = x->gr;
+  if(!same_shape_e(bb, x) || bb->prec != x->prec) return MXG_EINVAL;
+  return mxk_edge_gs_point(g->n, x->m, g->K, g->ph, kap_of(g), a, b, dir, x->prec, bb->d, x->d, g->st);
+}
+
+int gsforward_simple_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x)
+{
+  return gs_simple(creal_(a), creal_(b), bb, x, 0);
+}
+int gsbackward_simple_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x)
+{
+  return gs_simple(creal_(a), creal_(b), bb, x, 1);
+}
+int gssymm_simple_edge2d_gpu(mxg_field a, mxg_field b, const edge2d_gpu *bb, edge2d_gpu *x)
+{
+  return gs_simple(creal_(a), creal_(b), bb, x, 2);
+}
+
 int prolongation_edge2d_gpu(mxg_field alpha, const edge2d_gpu *c, edge2d_gpu *f)
 {
   if(f->gr->n != 2 * c->gr->n || c->m != f->m || c->prec != f->prec || c->gr->K != f->gr->K) return MXG_EINVAL;
@@ -448,6 +468,53 @@ int vcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2
     TRY(mxk_edge_prolong(g->n / 2, x[l]->m, g->K, g->ph, 1.0, x[l]->prec, x[l - 1]->d, x[l]->d, g->st));
     for(i = 0; i < nu; i++)
       TRY(mxk_edge_gs(g->n, x[l]->m, g->K, g->ph, kap_of(g), 1.0, 1.0, 1, x[l]->prec, b[l]->d, x[l]->d, g->st));
+  }
+  return (int) cudaStreamSynchronize(x[L]->gr->st);
+}
+
+int hcycle_edge2d_gpu(int L, int nu, const matrix_gpu *Ac, edge2d_gpu **b, edge2d_gpu **x, edge2d_gpu **d,
+                      node2d_gpu **bg, node2d_gpu **xg)
+{
+  /* hcycle_edge2d (edge2d.c:5756-5823) */
+  int l, i;
+  for(l = L; l > 0; l--) {
+    const grid2d_gpu *g = x[l]->gr;
+    for(i = 0; i < nu; i++)
+      TRY(gs_simple(1.0, 1.0, b[l], x[l], 0));
+    if(b[l]->prec != d[l]->prec) return MXG_EINVAL;
+    TRY(mxk_edge_apply(g->n, x[l]->m, g->K, g->ph, kap_of(g), -1.0, -1.0, 0, 1.0, x[l]->prec, x[l]->d,
+                       d[l]->prec, b[l]->d, d[l]->d, g->st));
+    TRY(mxk_adjgradient(g->n, x[l]->m, g->K, g->ph, 1.0, 0, 0.0, d[l]->prec, d[l]->d, bg[l]->prec, bg[l]->d, g->st));
+    TRY(zero_node2d_gpu(xg[l]));
+    for(i = 0; i < nu; i++)
+      TRY(mxk_node_gs(g->n, x[l]->m, g->K, g->ph, 1.0, 0, xg[l]->prec, bg[l]->d, xg[l]->d, g->st));
+    TRY(mxk_gradient(g->n, x[l]->m, g->K, g->ph, 1.0, xg[l]->prec, xg[l]->d, x[l]->prec, x[l]->d, g->st));
+    TRY(mxk_edge_apply(g->n, x[l]->m, g->K, g->ph, kap_of(g), -1.0, -1.0, 0, 1.0, x[l]->prec, x[l]->d,
+                       d[l]->prec, b[l]->d, d[l]->d, g->st));
+    TRY(zero_edge2d_gpu(b[l - 1]));
+    TRY(mxk_edge_restrict(g->n / 2, x[l]->m, g->K, g->ph, 1.0, d[l]->prec, d[l]->d, b[l - 1]->d, g->st));
+    TRY(zero_edge2d_gpu(x[l - 1]));
+  }
+  if(Ac) {
+    const grid2d_gpu *g = x[0]->gr;
+    if(!Ac->factored || Ac->rows != 2 * g->n * g->n || Ac->K != g->K) return MXG_EINVAL;
+    TRY(mxk_coarse_apply(Ac->rows, x[0]->m, g->K, Ac->d, 0, x[0]->prec, b[0]->d, x[0]->d, g->st));
+  }
+  else
+    for(i = 0; i < nu; i++)
+      TRY(gs_simple(1.0, 1.0, b[0], x[0], 2));
+  for(l = 1; l <= L; l++) {
+    const grid2d_gpu *g = x[l]->gr;
+    TRY(mxk_edge_prolong(g->n / 2, x[l]->m, g->K, g->ph, 1.0, x[l]->prec, x[l - 1]->d, x[l]->d, g->st));
+    TRY(mxk_edge_apply(g->n, x[l]->m, g->K, g->ph, kap_of(g), -1.0, -1.0, 0, 1.0, x[l]->prec, x[l]->d,
+                       d[l]->prec, b[l]->d, d[l]->d, g->st));
+    TRY(mxk_adjgradient(g->n, x[l]->m, g->K, g->ph, 1.0, 0, 0.0, d[l]->prec, d[l]->d, bg[l]->prec, bg[l]->d, g->st));
+    TRY(zero_node2d_gpu(xg[l]));
+    for(i = 0; i < nu; i++)
+      TRY(mxk_node_gs(g->n, x[l]->m, g->K, g->ph, 1.0, 1, xg[l]->prec, bg[l]->d, xg[l]->d, g->st));
+    TRY(mxk_gradient(g->n, x[l]->m, g->K, g->ph, 1.0, xg[l]->prec, xg[l]->d, x[l]->prec, x[l]->d, g->st));
+    for(i = 0; i < nu; i++)
+      TRY(gs_simple(1.0, 1.0, b[l], x[l], 1));
   }
   return (int) cudaStreamSynchronize(x[L]->gr->st);
 }

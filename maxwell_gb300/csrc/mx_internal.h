@@ -56,6 +56,11 @@ int mxk_edge_gs(int n, int m, int K, const double *phases, mxk_kappa kap,
 int mxk_edge_gs_colour(int n, int m, int K, const double *phases, mxk_kappa kap,
                        double alpha, double beta, int dir, int prec,
                        const void *b, void *x, mx_stream s);
+/* point Gauss-Seidel of alpha A + beta M in the reference's interleaved row
+ * order (gs*_simple_edge2d); dir 0 forward, 1 backward, 2 both */
+int mxk_edge_gs_point(int n, int m, int K, const double *phases, mxk_kappa kap,
+                      double alpha, double beta, int dir, int prec,
+                      const void *b, void *x, mx_stream s);
 int mxk_edge_prolong(int nc, int m, int K, const double *phases, double alpha,
                      int prec, const void *c, void *f, mx_stream s);
 int mxk_edge_restrict(int nc, int m, int K, const double *phases, double alpha,

@@ -54,6 +54,7 @@ struct mxg_solver {
   float *kf[MAXL], *kdd[MAXL];
   void *kafw[MAXL];                  /* AFW patch factors (alpha = beta = 1) */
   double *ph;                        /* phase table (mxk_phase_bytes) */
+  double *ph2;                       /* phase table of a subset of the slots (continuity) */
   int *gamma;                        /* K flags */
   void *b[MAXL], *x[MAXL], *d[MAXL];
   void *bg[MAXL], *xg[MAXL], *dg[MAXL];
@@ -72,6 +73,7 @@ struct mxg_solver {
   double *h_ph, *h_stats, *h_mu, *h_res, *h_rq;
   int *h_sel, *h_info, *h_conv, *h_steps;
   int have_prev, K_prev;              /* waves stored in Eprev (0..3) and their width */
+  int last_nk;                        /* k-points of the last mxg_bloch_solve */
   double last_ms;
   long launches;
   /* CUDA-event timing of the finest level's node Gauss-Seidel sweeps, AFW
@@ -130,7 +132,7 @@ void mxg_solver_free(mxg_solver *s)
     cudaFree(s->b[l]); cudaFree(s->x[l]); cudaFree(s->d[l]);
     cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
   }
-  cudaFree(s->ph); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv); cudaFree(s->ae_inv_f); cudaFree(s->an_inv_f);
+  cudaFree(s->ph); cudaFree(s->ph2); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv); cudaFree(s->ae_inv_f); cudaFree(s->an_inv_f);
   cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn);
   cudaFree(s->Eprev[0]); cudaFree(s->Eprev[1]); cudaFree(s->Eprev[2]);
   cudaFree(s->ga); cudaFree(s->gm); cudaFree(s->coef); cudaFree(s->theta); cudaFree(s->rwork);
@@ -161,7 +163,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   size_t es_g, es_e;
   double *kk[MAXL];
   if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 32
-     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 1
+     || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 2
      || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'))
     return 0;
   s = calloc(1, sizeof(mxg_solver));
@@ -219,7 +221,8 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
        || dalloc(&s->bg[l], nlen(s, l) * es_g) || dalloc(&s->xg[l], nlen(s, l) * es_g)
        || dalloc(&s->dg[l], nlen(s, l) * es_g))
       goto fail;
-  if(dalloc((void **) &s->ph, mxk_phase_bytes(K)) || dalloc((void **) &s->gamma, sizeof(int) * K)
+  if(dalloc((void **) &s->ph, mxk_phase_bytes(K)) || dalloc((void **) &s->ph2, mxk_phase_bytes(K))
+     || dalloc((void **) &s->gamma, sizeof(int) * K)
      || dalloc((void **) &s->ae_inv, sizeof(double) * 2 * (size_t) N0e * N0e * K)
      || dalloc((void **) &s->an_inv, sizeof(double) * 2 * (size_t) N0n * N0n * K)
      || dalloc(&s->ae_inv_f, sizeof(float) * 2 * (size_t) N0e * N0e * K)
@@ -480,12 +483,49 @@ static int lift(mxg_solver *s, int l, int py, void *y)
   return 0;
 }
 
+/* hcycle_edge2d (edge2d.c:5756-5823) on b[top], x[top]: point Gauss-Seidel
+ * plus a correction in the gradients on every level (the node vectors of
+ * the lifting serve as its work space) */
+static int hcycle_e(mxg_solver *s, int top)
+{
+  int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
+  for(l = top; l >= 1; l--) {
+    int n = s->n[l];
+    for(i = 0; i < nu; i++)
+      L_(mxk_edge_gs_point(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 0, pg, s->b[l], s->x[l], s->st));
+    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
+    L_(mxk_adjgradient(n, m, K, s->ph, 1.0, 0, 0.0, pg, s->d[l], pg, s->bg[l], s->st));
+    L_(mxk_zero(pg, s->xg[l], nlen(s, l), s->st));
+    for(i = 0; i < nu; i++)
+      TRY(node_gs(s, l, 0));
+    L_(mxk_gradient(n, m, K, s->ph, 1.0, pg, s->xg[l], pg, s->x[l], s->st));
+    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
+    L_(mxk_zero(pg, s->b[l - 1], elen(s, l - 1), s->st));
+    L_(mxk_edge_restrict(n / 2, m, K, s->ph, 1.0, pg, s->d[l], s->b[l - 1], s->st));
+    L_(mxk_zero(pg, s->x[l - 1], elen(s, l - 1), s->st));
+  }
+  L_(mxk_coarse_apply(2 * s->n0 * s->n0, m, K, s->ae_inv, s->ae_inv_f, pg, s->b[0], s->x[0], s->st));
+  for(l = 1; l <= top; l++) {
+    int n = s->n[l];
+    L_(mxk_edge_prolong(n / 2, m, K, s->ph, 1.0, pg, s->x[l - 1], s->x[l], s->st));
+    L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
+    L_(mxk_adjgradient(n, m, K, s->ph, 1.0, 0, 0.0, pg, s->d[l], pg, s->bg[l], s->st));
+    L_(mxk_zero(pg, s->xg[l], nlen(s, l), s->st));
+    for(i = 0; i < nu; i++)
+      TRY(node_gs(s, l, 1));
+    L_(mxk_gradient(n, m, K, s->ph, 1.0, pg, s->xg[l], pg, s->x[l], s->st));
+    for(i = 0; i < nu; i++)
+      L_(mxk_edge_gs_point(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 1, pg, s->b[l], s->x[l], s->st));
+  }
+  return 0;
+}
+
 static int precondition_body(mxg_solver *s, int l)
 {
   int i;
   L_(mxk_zero(s->pg, s->x[l], elen(s, l), s->st));
   for(i = 0; i < s->o.prec_steps; i++)
-    TRY(vcycle_e(s, l));
+    TRY(s->o.smoother == 2 ? hcycle_e(s, l) : vcycle_e(s, l));
   return 0;
 }
 
@@ -861,6 +901,7 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
     s->K_prev = K;
   }
   s->last_ms = total;
+  s->last_nk = nk;
   if(s->timing) {
     int q;
     if(s->restarts) fprintf(stderr, "%d warm-started wave(s) solved again cold\n", s->restarts);
@@ -953,6 +994,181 @@ int mxg_solver_check_fp64(mxg_solver *s, double *res)
       res[k * m + i] = sqrt(st[0] > 0.0 ? st[0] : 0.0) / (fabs(mu) * sqrt(st[1]) + 1e-300);
     }
   return upload_mu(s);
+}
+
+/* ------------------------------------------------------------------ */
+/* eigenvector continuity and Chern partial sums (exp_bloch2d.c:1058-1216) */
+/* ------------------------------------------------------------------ */
+
+/* An adjustment of one k-point's block: adjusted vector i = d[i] * raw
+ * vector perm[i] (a permutation with unit phases). */
+typedef struct {
+  int *perm;
+  mxg_field *d;
+} adjust_t;
+
+/* entry (row a*m + i, column b*m + j) of one k-point's column-major
+ * complex Gram matrix of ns columns: (block a, col i)^H M (block b, col j) */
+static mxg_field gram_at(const double *g, int ns, int m, int a, int i, int b, int j)
+{
+  size_t o = 2 * ((size_t) (b * m + j) * ns + (size_t) (a * m + i));
+  return g[o] + I * g[o + 1];
+}
+
+/* Mass Gram matrices of [E_l, E_{l-1}, E_{l-2}] under M(k_l) for the slots
+ * l = l0 .. l0 + cnt - 1 (nb = 3, or 2 when l0 = 1: [E_1, E_0]), from the
+ * complex128 copy of the block in En, with a phase table of just those
+ * slots; the matrices go to host (cnt * ns * ns complex). */
+static int continuity_grams(mxg_solver *s, int l0, int cnt, int nb, double *host)
+{
+  int m = s->m, ns = nb * m, q, k, pr[3], e;
+  const void *pp[3];
+  size_t slot = elen(s, s->L) / s->K * mxk_elem_size(MX_C128);
+  double *tab = malloc(mxk_phase_bytes(cnt));
+  if(!tab) return MXG_ENOMEM;
+  for(k = 0; k < cnt; k++)
+    memcpy(tab + 4 * k, s->h_ph + 4 * (l0 + k), sizeof(double) * 4);
+  mxk_phase_fill(cnt, tab);
+  e = (int) cudaMemcpyAsync(s->ph2, tab, mxk_phase_bytes(cnt), cudaMemcpyHostToDevice, s->st);
+  for(q = 0; q < nb; q++) {
+    pr[q] = MX_C128;
+    pp[q] = (const char *) s->En + (size_t) (l0 - q) * slot;
+  }
+  if(!e) e = mxk_block_gram(s->n[s->L], m, cnt, s->ph2, kap(s, s->L), nb, pr, pp, 0, 0, s->ga, s->gm,
+                            s->gscratch, s->gscratch_bytes, s->st);
+  s->launches += 2;
+  if(!e) e = (int) cudaMemcpyAsync(host, s->gm, sizeof(double) * 2 * (size_t) ns * ns * cnt, cudaMemcpyDeviceToHost,
+                                   s->st);
+  if(!e) e = (int) cudaStreamSynchronize(s->st);
+  free(tab);
+  return e;
+}
+
+int mxg_bloch_continuity(mxg_solver *s, int nk, const int *vertex, int continuity, int chern_vectors,
+                         double *lambda, mxg_field *chern, int *sign)
+{
+  int m = s->m, K = s->K, ie = s->o.ieigs, l, i, j, swaps = 0, e = 0;
+  int ns3 = 3 * m, ns2 = 2 * m;
+  double *g1, *g3 = 0, *coef;
+  adjust_t *Q;
+  mxg_field *ch;
+  if(!s || nk < 1 || nk > K || nk != s->last_nk || !vertex || chern_vectors < 0 || chern_vectors > ie
+     || (continuity != 'n' && continuity != 's' && continuity != 'r'))
+    return MXG_EINVAL;
+  TRY((int) cudaSetDevice(s->device));
+  g1 = malloc(sizeof(double) * 2 * ns2 * ns2);
+  if(nk > 2) g3 = malloc(sizeof(double) * 2 * (size_t) ns3 * ns3 * (nk - 2));
+  coef = calloc(2 * (size_t) m * m * K, sizeof(double));
+  Q = calloc(nk, sizeof(adjust_t));
+  ch = calloc(chern_vectors > 0 ? chern_vectors : 1, sizeof(mxg_field));
+  if(!g1 || (nk > 2 && !g3) || !coef || !Q || !ch) { e = MXG_ENOMEM; goto out; }
+  for(l = 0; l < nk; l++) {
+    Q[l].perm = malloc(sizeof(int) * m);
+    Q[l].d = malloc(sizeof(mxg_field) * m);
+    if(!Q[l].perm || !Q[l].d) { e = MXG_ENOMEM; goto out; }
+    for(i = 0; i < m; i++) { Q[l].perm[i] = i; Q[l].d[i] = 1.0; }
+  }
+  /* the raw blocks in complex128, and their mass Gram matrices */
+  if((e = mxk_convert(s->pe, s->E, MX_C128, s->En, elen(s, s->L), s->st))) goto out;
+  if(nk > 1 && (e = continuity_grams(s, 1, 1, 2, g1))) goto out;
+  if(nk > 2 && (e = continuity_grams(s, 2, nk - 2, 3, g3))) goto out;
+  for(i = 0; i < chern_vectors; i++) chern[i] = 0.0;
+  if(sign) sign[0] = 0;
+  for(l = 1; l < nk; l++) {
+    /* block a of the Gram: 0 this k-point, 1 the one before, 2 the one before that */
+    const double *G = l == 1 ? g1 : g3 + 2 * (size_t) ns3 * ns3 * (l - 2);
+    int ns = l == 1 ? ns2 : ns3;
+    int oldvertex = vertex[l - 1];
+    adjust_t *P1 = &Q[l - 1], *P2 = l > 1 ? &Q[l - 2] : 0, *P = &Q[l];
+    /* e_j^H M eold0_i for raw e_j: X01[j][perm1[i]] d1[i]; likewise eold1,
+     * which is zero at the second point (exp_bloch2d.c:773-777 clears it) */
+#define C0(jr, i) (gram_at(G, ns, m, 0, (jr), 1, P1->perm[i]) * P1->d[i])
+#define C1(jr, i) (P2 ? gram_at(G, ns, m, 0, (jr), 2, P2->perm[i]) * P2->d[i] : 0.0)
+    if(continuity == 'r') {
+      /* reorder: greedy, the raw vector closest to the (extrapolated) guess */
+      for(i = 0; i < ie; i++) {
+        double opt = -1.0;
+        int best = i;
+        for(j = i; j < ie; j++) {
+          int jr = P->perm[j];
+          double a = oldvertex ? cabs(C0(jr, i)) : cabs(2.0 * C0(jr, i) - C1(jr, i));
+          if(a > opt) { opt = a; best = j; }
+        }
+        if(best != i) {
+          int t = P->perm[i];
+          double tl;
+          P->perm[i] = P->perm[best];
+          P->perm[best] = t;
+          tl = lambda[(size_t) l * m + i];
+          lambda[(size_t) l * m + i] = lambda[(size_t) l * m + best];
+          lambda[(size_t) l * m + best] = tl;
+          swaps++;
+        }
+      }
+    }
+    if(continuity == 's' || continuity == 'r')
+      /* sign (phase): make e_i^H M guess_i real and positive */
+      for(i = 0; i < m; i++) {
+        int jr = P->perm[i];
+        mxg_field p = oldvertex ? C0(jr, i) : 2.0 * C0(jr, i) - C1(jr, i);
+        P->d[i] = cabs(p) > 0.0 ? p / cabs(p) : 1.0;
+      }
+    /* Chern partial sums with the adjusted vectors e'_i = d_i e_perm[i] */
+    for(i = 0; i < chern_vectors; i++) {
+      mxg_field o0e = conj(P1->d[i]) * gram_at(G, ns, m, 1, P1->perm[i], 0, P->perm[i]) * P->d[i];
+      mxg_field chup;
+      if(oldvertex) {
+        mxg_field o00 = conj(P1->d[i]) * gram_at(G, ns, m, 1, P1->perm[i], 1, P1->perm[i]) * P1->d[i];
+        chup = 0.5 * I * (o0e - o00);
+      }
+      else {
+        mxg_field o01 = P2 ? conj(P1->d[i]) * gram_at(G, ns, m, 1, P1->perm[i], 2, P2->perm[i]) * P2->d[i] : 0.0;
+        chup = 0.5 * I * (o0e - o01);
+        if(vertex[l]) {
+          mxg_field ee = conj(P->d[i]) * gram_at(G, ns, m, 0, P->perm[i], 0, P->perm[i]) * P->d[i];
+          mxg_field e0 = conj(P->d[i]) * gram_at(G, ns, m, 0, P->perm[i], 1, P1->perm[i]) * P1->d[i];
+          chup += 0.5 * I * (ee - e0);
+        }
+      }
+      ch[i] += chup;
+      chern[(size_t) l * chern_vectors + i] = ch[i];
+    }
+    if(sign) sign[l] = swaps;
+#undef C0
+#undef C1
+  }
+  /* apply the adjustments to the eigenvectors on the device: column i of
+   * k-point l becomes d_i times raw column perm_i */
+  for(l = 0; l < K; l++)
+    for(i = 0; i < m; i++) {
+      double *c;
+      int r = l < nk ? Q[l].perm[i] : i;
+      mxg_field d = l < nk ? Q[l].d[i] : 1.0;
+      c = coef + 2 * ((size_t) l * m * m + (size_t) i * m + r);
+      c[0] = creal(d);
+      c[1] = cimag(d);
+    }
+  e = (int) cudaMemcpyAsync(s->coef, coef, sizeof(double) * 2 * (size_t) m * m * K, cudaMemcpyHostToDevice, s->st);
+  if(!e) {
+    int pr = s->pe;
+    const void *pp = s->E;
+    e = mxk_block_combine(s->n[s->L], m, K, 1, &pr, &pp, s->coef, m, 0, s->combw, s->pe, s->En, s->st);
+    s->launches += 2;
+  }
+  if(!e) {
+    swapp(&s->E, &s->En);
+    e = (int) cudaStreamSynchronize(s->st);
+  }
+  /* the adjusted Rayleigh quotients follow the reordering */
+  if(!e)
+    for(l = 0; l < nk; l++)
+      for(i = 0; i < m; i++)
+        s->h_rq[l * m + i] = lambda[(size_t) l * m + i] + 1.0;
+out:
+  if(Q)
+    for(l = 0; l < nk; l++) { free(Q[l].perm); free(Q[l].d); }
+  free(Q); free(g1); free(g3); free(coef); free(ch);
+  return e;
 }
 
 int mxg_solver_restarts(const mxg_solver *s)

@@ -399,6 +399,52 @@ __global__ void k_edge_gs_rows(int n, int m, int K, const double* __restrict__ p
 }
 
 // ------------------------------------------------------------------
+// Point Gauss-Seidel of alpha A + beta M, edge by edge, in the reference's
+// interleaved row order (gsforward/gsbackward_simple_edge2d with
+// SMOOTHER_INTERLEAVED, edge2d.c:3890-5573): forward, row 0, the even rows,
+// the odd rows, row n-1, each left to right, x-edge (i,j) then y-edge
+// (i,j); backward the exact reverse.  An edge's update is its residual row
+// divided by its diagonal, axy (kappa of its two cells) + 4 beta/6.  Row j
+// reads rows j-1..j+1 only, so the rows of one parity are independent and
+// the sweep is two launches (rows 0, 2, .., n-2 and rows 1, 3, .., n-1),
+// one thread per (k, row, vector) walking its row.  The smoother of the
+// Hiptmair cycle (hcycle_edge2d).
+// ------------------------------------------------------------------
+template <typename S, typename R>
+__global__ void k_edge_gs_point(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap, Sc axy_s,
+                                Sc mm_s, int j0, int jstep, int nrows, int backward, const S* __restrict__ b,
+                                S* x) {
+  size_t t = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  size_t per_k = (size_t) nrows * m;
+  if (t >= per_k * K) return;
+  int k = (int) (t / per_k);
+  int r = (int) (t - (size_t) k * per_k);
+  int v = r % m;
+  int j = j0 + (r / m) * jstep;
+  Lay L{n, m, K};
+  S* xk = x + L.edge(k, 0, 0, 0, v);
+  const S* bk = b + L.edge(k, 0, 0, 0, v);
+  EAcc<S, R> X{xk, n, m, seam_load<R>(ph, K, k, n)};
+  const R axy = sget<R>(axy_s), mm = sget<R>(mm_s), four = rc<R>(4.0f), one = rc<R>(1.0f);
+  auto upd_x = [&](int i) {
+    size_t o = ((size_t) j * n + i) * m;
+    cx<R> res = Store<S, R>::ld(bk + o) - kx_x<R>(X, kap, axy, mm, i, j);
+    R diag = axy * (kap(i, j - 1) + kap(i, j)) + four * mm;
+    Store<S, R>::st(xk + o, Store<S, R>::ld(xk + o) + scal(one / diag, res));
+  };
+  auto upd_y = [&](int i) {
+    size_t o = ((size_t) (n + j) * n + i) * m;
+    cx<R> res = Store<S, R>::ld(bk + o) - kx_y<R>(X, kap, axy, mm, i, j);
+    R diag = axy * (kap(i - 1, j) + kap(i, j)) + four * mm;
+    Store<S, R>::st(xk + o, Store<S, R>::ld(xk + o) + scal(one / diag, res));
+  };
+  if (!backward)
+    for (int i = 0; i < n; i++) { upd_x(i); upd_y(i); }
+  else
+    for (int i = n - 1; i >= 0; i--) { upd_y(i); upd_x(i); }
+}
+
+// ------------------------------------------------------------------
 // AFW vertex-patch smoother in four colours.  The vertices (i, j) split by
 // (i mod 2, j mod 2); two patches of one colour share no unknown, and none
 // reads an unknown the other writes (a patch writes x(i-1..i, j) and
@@ -1293,6 +1339,34 @@ extern "C" int mxk_edge_apply(int n, int m, int K, const double* ph, mxk_kappa k
 // 1..n-3, row n-1 (edge2d.c:2656-2758).  Row 0 commutes with the other even
 // rows and row n-1 with the other odd rows (n even), so two phases of
 // concurrent rows reproduce it; backward is the exact reverse.
+template <typename S, typename R>
+static int L_edge_gs_point(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha, double beta,
+                           int j0, int backward, const void* b, void* x, cudaStream_t st) {
+  size_t work = (size_t) (n / 2) * m * K;
+  k_edge_gs_point<S, R><<<nblocks(work, 64), 64, 0, st>>>(n, m, K, ph, make_kap<R>(kap, n),
+                                                          make_sc(alpha * (double) n * (double) n),
+                                                          make_sc(beta / 6.0), j0, 2, n / 2, backward,
+                                                          (const S*) b, (S*) x);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
+extern "C" int mxk_edge_gs_point(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
+                                 double beta, int dir, int prec, const void* b, void* x, mx_stream s) {
+  cudaStream_t st = (cudaStream_t) s;
+  int e;
+  if (n < 2 || (n & 1)) return (int) cudaErrorInvalidValue;
+  if (dir == 0 || dir == 2) {
+    if ((e = MX_BY_PREC(prec, L_edge_gs_point, n, m, K, ph, kap, alpha, beta, 0, 0, b, x, st))) return e;
+    if ((e = MX_BY_PREC(prec, L_edge_gs_point, n, m, K, ph, kap, alpha, beta, 1, 0, b, x, st))) return e;
+  }
+  if (dir == 1 || dir == 2) {
+    if ((e = MX_BY_PREC(prec, L_edge_gs_point, n, m, K, ph, kap, alpha, beta, 1, 1, b, x, st))) return e;
+    if ((e = MX_BY_PREC(prec, L_edge_gs_point, n, m, K, ph, kap, alpha, beta, 0, 1, b, x, st))) return e;
+  }
+  return 0;
+}
+
 extern "C" int mxk_edge_gs(int n, int m, int K, const double* ph, mxk_kappa kap, double alpha,
                            double beta, int dir, int prec, const void* b, void* x, mx_stream s) {
   cudaStream_t st = (cudaStream_t) s;

@@ -400,6 +400,56 @@ om_gs_edge(int n, const double *kappa, cx xf, cx yf, cx alpha, cx beta,
     gs_edge_dir(n, kappa, xf, yf, alpha, beta, 1, b, x);
 }
 
+/* Point Gauss-Seidel of alpha A + beta M in the reference's interleaved
+ * row order (gsforward/gsbackward_simple_edge2d, edge2d.c:3890-5573, the
+ * variant compiled with SMOOTHER_INTERLEAVED): forward row 0, rows
+ * 2, 4, .., n-2, rows 1, 3, .., n-3, row n-1, each left to right with the
+ * x-edge (i,j) before the y-edge (i,j); backward the reverse.  Each edge
+ * moves by its residual row over its diagonal axy (kappa of its two cells)
+ * + 4 beta/6. */
+static void
+gs_simple_row(int n, const double *kappa, cx xf, cx yf, cx axy, cx mm, const cx *b, cx *x, int j, int back)
+{
+  long nn = (long) n * n;
+  int s, i;
+  for(s = 0; s < n; s++) {
+    int q;
+    i = back ? n - 1 - s : s;
+    for(q = 0; q < 2; q++) {
+      int ydir = back ? q == 0 : q == 1;
+      if(!ydir) {
+        cx r = b[i + j * n] - kx_xedge(n, kappa, xf, yf, axy, mm, x, i, j);
+        cx d = axy * (kap(kappa, n, i, j - 1) + kap(kappa, n, i, j)) + 4.0 * mm;
+        x[i + j * n] += r / d;
+      }
+      else {
+        cx r = b[nn + i + j * n] - kx_yedge(n, kappa, xf, yf, axy, mm, x, i, j);
+        cx d = axy * (kap(kappa, n, i - 1, j) + kap(kappa, n, i, j)) + 4.0 * mm;
+        x[nn + i + j * n] += r / d;
+      }
+    }
+  }
+}
+
+void
+om_gs_edge_simple(int n, const double *kappa, cx xf, cx yf, cx alpha, cx beta, int dir, const cx *b, cx *x)
+{
+  cx axy = alpha * (double) n * (double) n, mm = beta / 6.0;
+  int j;
+  if(dir == 0 || dir == 2) {
+    gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, 0, 0);
+    for(j = 2; j < n - 1; j += 2) gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, j, 0);
+    for(j = 1; j < n - 1; j += 2) gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, j, 0);
+    gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, n - 1, 0);
+  }
+  if(dir == 1 || dir == 2) {
+    gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, n - 1, 1);
+    for(j = 1; j < n - 1; j += 2) gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, j, 1);
+    for(j = 2; j < n - 1; j += 2) gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, j, 1);
+    gs_simple_row(n, kappa, xf, yf, axy, mm, b, x, 0, 1);
+  }
+}
+
 /* The four-colour order of the same patch solves (the GPU solver's
  * smoother; it has no counterpart in the reference): vertices split by
  * (i mod 2, j mod 2), forward (0,0), (1,0), (0,1), (1,1), backward the
@@ -1063,6 +1113,65 @@ om_vcycle_edge(om_mg *h, int L, int nu, int coarse, const cx *b, cx *x)
   memcpy(x, h->x[L], sizeof(cx) * 2 * (size_t) (h->n0 << L) * (h->n0 << L));
 }
 
+/* The Hiptmair cycle (hcycle_edge2d, edge2d.c:5756-5823): per level down,
+ * nu forward point GS sweeps, then a correction in the gradients (G of nu
+ * forward node GS sweeps on G^H of the residual), the residual restricted;
+ * the coarse dense solve (or nu symmetric point GS sweeps); per level up,
+ * the prolongated correction, a gradient correction with backward node
+ * sweeps and nu backward point GS sweeps. */
+void
+om_hcycle_edge(om_mg *h, int L, int nu, int coarse, const cx *b, cx *x)
+{
+  int l, s, n;
+  long len;
+  cx xf = h->xf, yf = h->yf;
+  memcpy(h->b[L], b, sizeof(cx) * 2 * (size_t) (h->n0 << L) * (h->n0 << L));
+  memcpy(h->x[L], x, sizeof(cx) * 2 * (size_t) (h->n0 << L) * (h->n0 << L));
+  for(l = L; l > 0; l--) {
+    n = h->n0 << l;
+    len = 2L * n * n;
+    for(s = 0; s < nu; s++)
+      om_gs_edge_simple(n, h->kappa[l], xf, yf, 1.0, 1.0, 0, h->b[l], h->x[l]);
+    memcpy(h->d[l], h->b[l], sizeof(cx) * len);
+    om_addeval_edge(n, h->kappa[l], xf, yf, -1.0, -1.0, h->x[l], h->d[l]);
+    memset(h->bg[l], 0, sizeof(cx) * len / 2);
+    om_adjgradient(n, xf, yf, 1.0, h->d[l], h->bg[l]);
+    memset(h->xg[l], 0, sizeof(cx) * len / 2);
+    for(s = 0; s < nu; s++)
+      om_gs_node(n, xf, yf, 1.0, 0, h->bg[l], h->xg[l]);
+    om_gradient(n, xf, yf, 1.0, h->xg[l], h->x[l]);
+    memcpy(h->d[l], h->b[l], sizeof(cx) * len);
+    om_addeval_edge(n, h->kappa[l], xf, yf, -1.0, -1.0, h->x[l], h->d[l]);
+    memset(h->b[l - 1], 0, sizeof(cx) * len / 4);
+    om_restrict_edge(n / 2, xf, yf, 1.0, h->d[l], h->b[l - 1]);
+    memset(h->x[l - 1], 0, sizeof(cx) * len / 4);
+  }
+  n = h->n0;
+  if(coarse) {
+    memcpy(h->x[0], h->b[0], sizeof(cx) * 2 * n * n);
+    om_potrs(2 * n * n, h->Ae, h->x[0]);
+  }
+  else
+    for(s = 0; s < nu; s++)
+      om_gs_edge_simple(n, h->kappa[0], xf, yf, 1.0, 1.0, 2, h->b[0], h->x[0]);
+  for(l = 1; l <= L; l++) {
+    n = h->n0 << l;
+    len = 2L * n * n;
+    om_prolong_edge(n / 2, xf, yf, 1.0, h->x[l - 1], h->x[l]);
+    memcpy(h->d[l], h->b[l], sizeof(cx) * len);
+    om_addeval_edge(n, h->kappa[l], xf, yf, -1.0, -1.0, h->x[l], h->d[l]);
+    memset(h->bg[l], 0, sizeof(cx) * len / 2);
+    om_adjgradient(n, xf, yf, 1.0, h->d[l], h->bg[l]);
+    memset(h->xg[l], 0, sizeof(cx) * len / 2);
+    for(s = 0; s < nu; s++)
+      om_gs_node(n, xf, yf, 1.0, 1, h->bg[l], h->xg[l]);
+    om_gradient(n, xf, yf, 1.0, h->xg[l], h->x[l]);
+    for(s = 0; s < nu; s++)
+      om_gs_edge_simple(n, h->kappa[l], xf, yf, 1.0, 1.0, 1, h->b[l], h->x[l]);
+  }
+  memcpy(x, h->x[L], sizeof(cx) * 2 * (size_t) (h->n0 << L) * (h->n0 << L));
+}
+
 void
 om_vcycle_node(om_mg *h, int L, int nu, int coarse, const cx *b, cx *x)
 {
@@ -1561,6 +1670,93 @@ om_bloch_solve_timed(const om_opts *o, const double *kappa_fine, int nk,
   free(c.t1); free(c.t2); free(c.tn);
   om_mg_free(h);
   return status;
+}
+
+/* Eigenvector continuity and Chern partial sums along consecutive
+ * k-points, as the reference's Bloch scan does them after each point
+ * (exp_bloch2d.c:1058-1216): vecs holds nk blocks of m vectors (len each),
+ * adjusted in place; eold0 / eold1 are the adjusted blocks of the two points
+ * before (eold1 zero at the second point, exp_bloch2d.c:773-777); every mass
+ * product is taken with the current point's Bloch factors. */
+void
+om_continuity(int n, int nk, const cx *xfs, const cx *yfs, int m, int ieigs, const int *vertex,
+              int continuity, int chern_vectors, cx *vecs, double *lambda, cx *chern, int *sign)
+{
+  long len = 2L * n * n, q;
+  cx *x = malloc(sizeof(cx) * len), *zero = calloc(len, sizeof(cx));
+  cx *chs = calloc(chern_vectors > 0 ? chern_vectors : 1, sizeof(cx));
+  int l, i, j, swaps = 0;
+  for(i = 0; i < chern_vectors; i++) chern[i] = 0.0;
+  if(sign) sign[0] = 0;
+  for(l = 1; l < nk; l++) {
+    cx *e = vecs + (size_t) l * m * len, *e0 = vecs + (size_t) (l - 1) * m * len;
+    cx *e1 = l > 1 ? vecs + (size_t) (l - 2) * m * len : 0;
+    int oldvertex = vertex[l - 1];
+#define EV(b, i) ((b) ? (b) + (size_t) (i) * len : zero)
+#define MP(a, b) om_massprod_edge(n, xfs[l], yfs[l], (a), (b))
+    if(continuity == 'r')
+      for(i = 0; i < ieigs; i++) {
+        double opt, a;
+        int k = i;
+        if(oldvertex)
+          memcpy(x, EV(e0, i), sizeof(cx) * len);
+        else {
+          for(q = 0; q < len; q++) x[q] = 2.0 * EV(e0, i)[q] - EV(e1, i)[q];
+          a = sqrt(creal(MP(x, x)));
+          for(q = 0; q < len; q++) x[q] /= a;
+        }
+        opt = cabs(MP(EV(e, i), x));
+        for(j = i + 1; j < ieigs; j++) {
+          a = cabs(MP(EV(e, j), x));
+          if(a > opt) { k = j; opt = a; }
+        }
+        if(k != i) {
+          double tl;
+          for(q = 0; q < len; q++) {
+            cx t = EV(e, i)[q];
+            EV(e, i)[q] = EV(e, k)[q];
+            EV(e, k)[q] = t;
+          }
+          tl = lambda[(size_t) l * m + i];
+          lambda[(size_t) l * m + i] = lambda[(size_t) l * m + k];
+          lambda[(size_t) l * m + k] = tl;
+          swaps++;
+        }
+      }
+    if(continuity == 's' || continuity == 'r')
+      for(i = 0; i < m; i++) {
+        cx p;
+        if(oldvertex)
+          p = MP(EV(e, i), EV(e0, i));
+        else {
+          for(q = 0; q < len; q++) x[q] = 2.0 * EV(e0, i)[q] - EV(e1, i)[q];
+          p = MP(EV(e, i), x);
+        }
+        p /= cabs(p);
+        for(q = 0; q < len; q++) EV(e, i)[q] *= p;
+      }
+    for(i = 0; i < chern_vectors; i++) {
+      cx chup;
+      if(oldvertex) {
+        for(q = 0; q < len; q++) x[q] = EV(e, i)[q] - EV(e0, i)[q];
+        chup = 0.5 * I * MP(EV(e0, i), x);
+      }
+      else {
+        for(q = 0; q < len; q++) x[q] = EV(e, i)[q] - EV(e1, i)[q];
+        chup = 0.5 * I * MP(EV(e0, i), x);
+        if(vertex[l]) {
+          for(q = 0; q < len; q++) x[q] = EV(e, i)[q] - EV(e0, i)[q];
+          chup += 0.5 * I * MP(EV(e, i), x);
+        }
+      }
+      chs[i] += chup;
+      chern[(size_t) l * chern_vectors + i] = chs[i];
+    }
+    if(sign) sign[l] = swaps;
+#undef EV
+#undef MP
+  }
+  free(x); free(zero); free(chs);
 }
 
 /* d lambda_i / d eps_c = -axy kappa_c^2 |curl_c e_i|^2 for M-normalised e_i

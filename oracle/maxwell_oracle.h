@@ -32,6 +32,9 @@ double om_norm2(long len, const om_cplx *x);
 void om_gs_edge(int n, const double *kappa, om_cplx xf, om_cplx yf,
                 om_cplx alpha, om_cplx beta, int dir,
                 const om_cplx *b, om_cplx *x);
+/* point Gauss-Seidel in the reference's interleaved row order (gs*_simple_edge2d) */
+void om_gs_edge_simple(int n, const double *kappa, om_cplx xf, om_cplx yf,
+                       om_cplx alpha, om_cplx beta, int dir, const om_cplx *b, om_cplx *x);
 /* the same patch solves in four vertex colours (the GPU solver's order) */
 void om_gs_edge_colour(int n, const double *kappa, om_cplx xf, om_cplx yf,
                        om_cplx alpha, om_cplx beta, int dir, const om_cplx *b, om_cplx *x);
@@ -86,6 +89,9 @@ void om_vcycle_edge(om_mg *h, int l, int nu, int coarse,
                     const om_cplx *b, om_cplx *x);
 void om_vcycle_node(om_mg *h, int l, int nu, int coarse,
                     const om_cplx *b, om_cplx *x);
+/* the Hiptmair cycle (hcycle_edge2d) with the point smoother */
+void om_hcycle_edge(om_mg *h, int l, int nu, int coarse,
+                    const om_cplx *b, om_cplx *x);
 const double *om_mg_kappa(const om_mg *h, int l);
 
 /* ---- the per-k eigensolver flow ---- */
@@ -115,6 +121,13 @@ int om_bloch_solve_timed(const om_opts *o, const double *kappa_fine,
                          int nk, const om_cplx *xfs, const om_cplx *yfs,
                          double *lambda_out, int *steps_out, double *res_out,
                          om_cplx *evec_out, double *seconds_out);
+
+/* Eigenvector continuity ('n', 's', 'r') and Chern partial sums along nk
+ * consecutive k-points (exp_bloch2d.c:1058-1216); vecs and lambda adjusted
+ * in place, chern nk*chern_vectors partial sums, sign nk swap counts. */
+void om_continuity(int n, int nk, const om_cplx *xfs, const om_cplx *yfs, int m, int ieigs,
+                   const int *vertex, int continuity, int chern_vectors, om_cplx *vecs, double *lambda,
+                   om_cplx *chern, int *sign);
 
 /* Eigenvalue sensitivity with respect to the permittivity of every cell. */
 void om_eps_sensitivity(int n, const double *kappa, om_cplx xf, om_cplx yf,

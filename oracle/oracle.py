@@ -98,6 +98,12 @@ class Oracle:
                             _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
         return x
 
+    def gs_edge_simple(self, n, kappa, xf, yf, alpha, beta, direction, b, x):
+        x = _cvec(x).copy()
+        self.lib.om_gs_edge_simple(C.c_int(n), _p(np.ascontiguousarray(kappa, np.float64)), _cz(xf), _cz(yf),
+                                   _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
+        return x
+
     def gs_edge_colour(self, n, kappa, xf, yf, alpha, beta, direction, b, x):
         x = _cvec(x).copy()
         self.lib.om_gs_edge_colour(C.c_int(n), _p(np.ascontiguousarray(kappa, np.float64)), _cz(xf), _cz(yf),
@@ -244,6 +250,14 @@ class Oracle:
         self.lib.om_mg_free(h)
         return x
 
+    def hcycle_edge(self, n0, L, kappa_fine, xf, yf, nu, coarse, cycles, b, x):
+        h = self._mg(n0, L, kappa_fine, xf, yf)
+        x = _cvec(x).copy()
+        for _ in range(cycles):
+            self.lib.om_hcycle_edge(h, C.c_int(L), C.c_int(nu), C.c_int(coarse), _p(_cvec(b)), _p(x))
+        self.lib.om_mg_free(h)
+        return x
+
     def vcycle_node(self, n0, L, xf, yf, nu, coarse, cycles, b, x):
         n = n0 << L
         h = self._mg(n0, L, np.ones(n * n), xf, yf)
@@ -295,6 +309,21 @@ class Oracle:
             return st, lam, steps, res, ev, secs
         return st, lam, steps, res, ev
 
+    def continuity(self, n, factors, ieigs, vertex, continuity, chern_vectors, vecs, lam):
+        """om_continuity on copies: returns adjusted vectors, eigenvalues,
+        Chern partial sums (nk, chern_vectors) and swap counts (nk)."""
+        factors = np.asarray(factors, np.complex128)
+        nk, m = vecs.shape[0], vecs.shape[1]
+        v = np.ascontiguousarray(vecs, np.complex128).copy()
+        lam = np.ascontiguousarray(lam, np.float64).copy()
+        ch = np.zeros((nk, max(chern_vectors, 1)), np.complex128)
+        sg = np.zeros(nk, np.int32)
+        self.lib.om_continuity(C.c_int(n), C.c_int(nk), _p(np.ascontiguousarray(factors[:, 0])),
+                               _p(np.ascontiguousarray(factors[:, 1])), C.c_int(m), C.c_int(ieigs),
+                               _p(np.ascontiguousarray(vertex, np.int32)), C.c_int(ord(continuity)),
+                               C.c_int(chern_vectors), _p(v), _p(lam), _p(ch), _p(sg))
+        return v, lam, ch[:, :chern_vectors], sg
+
     def eps_sensitivity(self, n, kappa, xf, yf, vecs, weights):
         vecs = np.ascontiguousarray(vecs, np.complex128)
         w = np.ascontiguousarray(weights, np.float64)
@@ -329,6 +358,19 @@ class RefLib:
         x = _cvec(x).copy()
         self.lib.ref_gs_edge2d(C.c_int(n), _p(np.ascontiguousarray(kappa, np.float64)), _cz(xf), _cz(yf),
                                _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
+        return x
+
+    def gs_edge_simple(self, n, kappa, xf, yf, alpha, beta, direction, b, x):
+        x = _cvec(x).copy()
+        self.lib.ref_gs_simple_edge2d(C.c_int(n), _p(np.ascontiguousarray(kappa, np.float64)), _cz(xf), _cz(yf),
+                                      _cz(alpha), _cz(beta), C.c_int(direction), _p(_cvec(b)), _p(x))
+        return x
+
+    def hcycle_edge(self, n0, L, kappa_fine, xf, yf, nu, coarse, cycles, b, x):
+        x = _cvec(x).copy()
+        self.lib.ref_hcycle_edge2d(C.c_int(n0), C.c_int(L), _p(np.ascontiguousarray(kappa_fine, np.float64)),
+                                   _cz(xf), _cz(yf), C.c_int(nu), C.c_int(coarse), C.c_int(cycles),
+                                   _p(_cvec(b)), _p(x))
         return x
 
     def transfer_edge(self, nc, xf, yf, alpha, restrict, a, out):

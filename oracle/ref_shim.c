@@ -101,6 +101,23 @@ ref_gs_edge2d(int n, const double *kappa, field xf, field yf,
   del_edge2d(eb); del_edge2d(ex); del_grid2d(gr);
 }
 
+/* the point smoother of the Hiptmair cycle: dir 0 forward, 1 backward, 2 symmetric */
+void
+ref_gs_simple_edge2d(int n, const double *kappa, field xf, field yf,
+                     field alpha, field beta, int dir, const field *b, field *x)
+{
+  grid2d *gr = mkgrid(n, kappa, xf, yf);
+  edge2d *eb = mkedge(gr, b), *ex = mkedge(gr, x);
+  if(dir == 0)
+    gsforward_simple_edge2d(alpha, beta, eb, ex);
+  else if(dir == 1)
+    gsbackward_simple_edge2d(alpha, beta, eb, ex);
+  else
+    gssymm_simple_edge2d(alpha, beta, eb, ex);
+  densefrom_edge2d(ex, x);
+  del_edge2d(eb); del_edge2d(ex); del_grid2d(gr);
+}
+
 /* nc: coarse intervals; the fine grid has 2*nc */
 void
 ref_transfer_edge2d(int nc, field xf, field yf, field alpha, int restrict_,
@@ -316,6 +333,21 @@ ref_vcycle_edge2d(int n0, int L, const double *kappa_fine, field xf, field yf,
   denseto_edge2d(x, h->x[L]);
   for(c = 0; c < cycles; c++)
     vcycle_edge2d(L, nu, coarse ? h->Ae : 0, h->b, h->x, h->d);
+  densefrom_edge2d(h->x[L], x);
+  delhier(h);
+}
+
+/* `cycles` Hiptmair cycles (hcycle_edge2d) on the finest level */
+void
+ref_hcycle_edge2d(int n0, int L, const double *kappa_fine, field xf, field yf,
+                  int nu, int coarse, int cycles, const field *b, field *x)
+{
+  hier *h = mkhier(n0, L, kappa_fine, xf, yf, coarse, 0);
+  int c;
+  denseto_edge2d(b, h->b[L]);
+  denseto_edge2d(x, h->x[L]);
+  for(c = 0; c < cycles; c++)
+    hcycle_edge2d(L, nu, coarse ? h->Ae : 0, h->b, h->x, h->d, h->bg, h->xg);
   densefrom_edge2d(h->x[L], x);
   delhier(h);
 }

@@ -5,7 +5,8 @@ Runs the reference's own modules (compiled unmodified by
 and writes ``tests/golden/*.npz``.  Needs the reference sources at build
 time; the fixtures it writes are committed so that the tests run anywhere.
 
-    OPENBLAS_NUM_THREADS=1 python tests/golden/gen_golden.py
+    OPENBLAS_NUM_THREADS=1 python tests/golden/gen_golden.py            # all fixtures
+    OPENBLAS_NUM_THREADS=1 python tests/golden/gen_golden.py hiptmair   # hiptmair_n16.npz only
 """
 from __future__ import annotations
 
@@ -131,13 +132,36 @@ def gen_eigs(R: RefLib) -> dict:
                 lam=lam, steps=steps, defects=dfc, tol=1e-9)
 
 
+def gen_hiptmair(R: RefLib, seed: int) -> dict:
+    """The point smoother (gs*_simple_edge2d) and the Hiptmair cycle
+    (hcycle_edge2d) on a 16^2 grid with a random kappa in one quadrant,
+    equal across the seams on every level (so that the reference's
+    matrix-free residuals use the kappa its dense matrix does)."""
+    rng = np.random.default_rng(seed)
+    n0, L = 4, 2
+    n = n0 << L
+    kap = quadrant_kappa(rng, n)
+    xf, yf = np.exp(0.9j), np.exp(-0.6j)
+    b, x = cvec(rng, 2 * n * n), cvec(rng, 2 * n * n)
+    out = dict(n0=n0, L=L, kappa=kap, xf=xf, yf=yf, b=b, x=x)
+    for d, name in ((0, "fwd"), (1, "bwd"), (2, "symm")):
+        out[f"simple_{name}"] = R.gs_edge_simple(n, kap, xf, yf, 1.0, 1.0, d, b, x)
+    out["hcycle"] = R.hcycle_edge(n0, L, kap, xf, yf, 2, 1, 2, b, np.zeros_like(b))
+    out["hcycle_nocoarse"] = R.hcycle_edge(n0, L, kap, xf, yf, 2, 0, 1, b, np.zeros_like(b))
+    return out
+
+
 def main() -> None:
     build_oracle(ref=True)
     R = RefLib()
+    if sys.argv[1:] == ["hiptmair"]:
+        np.savez_compressed(os.path.join(HERE, "hiptmair_n16.npz"), **gen_hiptmair(R, 21))
+        return
     np.savez_compressed(os.path.join(HERE, "ops_n8.npz"), **gen_ops(R, 8, 8))
     np.savez_compressed(os.path.join(HERE, "ops_n16.npz"), **gen_ops(R, 16, 16))
     np.savez_compressed(os.path.join(HERE, "vcycle_n16.npz"), **gen_vcycle(R, 3))
     np.savez_compressed(os.path.join(HERE, "eigs_n32_disc.npz"), **gen_eigs(R))
+    np.savez_compressed(os.path.join(HERE, "hiptmair_n16.npz"), **gen_hiptmair(R, 21))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

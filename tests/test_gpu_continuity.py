@@ -1,0 +1,46 @@
+"""Eigenvector continuity and Chern partial sums (mxg_bloch_continuity,
+exp_bloch2d.c:1058-1216) against the oracle's literal restatement of the
+reference's code applied to the same eigenvectors: the k-points of the
+reference driver's own curve (Kivshar disc, 16^2, 14 points with corners at
+points 0, 4, 8 and 13), solved by the GPU in one wave; the raw eigenvectors
+go to the oracle, the GPU adjusts its own.  Swap counts and the reordered
+eigenvalues agree exactly, the Chern partial sums and the adjusted
+eigenvectors to 1e-9."""
+import numpy as np
+import pytest
+
+import maxwell_gb300 as mx
+
+pytestmark = pytest.mark.gpu
+
+
+def curve_vertices(nk, steps_per_edge):
+    """blochcurve's corner flags (exp_bloch2d.c:45-46), with the first point
+    a corner as the scan starts (exp_bloch2d.c:447)."""
+    return np.array([1 if p in (0, steps_per_edge, 2 * steps_per_edge, nk - 1) else 0 for p in range(nk)],
+                    np.int32)
+
+
+@pytest.mark.parametrize("continuity", ["n", "s", "r"])
+def test_continuity_matches_oracle(oracle, golden, continuity):
+    g = golden("bloch_curve_n16_kivshar.npz")
+    n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
+    n = n0 << L
+    kap = oracle.disc_kappa(n, [g["disc"]], float(g["eps_base"]))
+    fac = g["factors"]
+    nk = len(fac)
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, wave=nk, relative=0, tol=1e-9,
+                  max_nested=40, max_steps=80)
+    lam, steps, res = s.solve(fac)
+    assert res[:, :ie].max() <= 1e-9
+    raw = s.eigenvectors()
+    vertex = curve_vertices(nk, 4)
+    lam_g, chern_g, sign_g = s.continuity(lam, vertex, continuity, chern_vectors=ie)
+    adj = s.eigenvectors()
+    v_o, lam_o, chern_o, sign_o = oracle.continuity(n, fac, ie, vertex, continuity, ie, raw, lam)
+    assert np.array_equal(sign_g, sign_o)
+    assert np.array_equal(lam_g, lam_o)
+    assert np.abs(chern_g - chern_o).max() < 1e-9
+    assert np.abs(adj - v_o).max() < 1e-9 * np.abs(v_o).max()
+    if continuity == "n":
+        assert np.array_equal(adj, raw)

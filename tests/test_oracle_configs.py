@@ -40,3 +40,26 @@ def test_oracle_matches_config1_reference(oracle, golden):
     assert st == 0
     want = g["lam"][pick, :ie]
     assert (np.abs(lam[:, :ie] - want) / want).max() < 1e-8
+
+
+def test_chern_sums_do_not_depend_on_the_eigenvector_phases(oracle, golden):
+    """The sign continuity absorbs any phase of the input eigenvectors: Chern
+    partial sums along the reference driver's curve are the same when every
+    eigenvector of every point is multiplied by a random unit phase."""
+    g = golden("bloch_curve_n16_kivshar.npz")
+    n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
+    n = n0 << L
+    kap = oracle.disc_kappa(n, [g["disc"]], float(g["eps_base"]))
+    fac = g["factors"]
+    st, lam, steps, res, vec = oracle.bloch_solve(kap, fac, n0=n0, L=L, ieigs=ie, m=m, method=1, max_nested=40,
+                                                  max_steps=80, tol=1e-9, relative=0, extrapolation="n", wave=1,
+                                                  want_vectors=True)
+    assert st == 0
+    nk = len(fac)
+    vertex = np.array([1 if p in (0, 4, 8, nk - 1) else 0 for p in range(nk)], np.int32)
+    _, _, ch1, _ = oracle.continuity(n, fac, ie, vertex, "s", ie, vec, lam)
+    rng = np.random.default_rng(3)
+    ph = np.exp(2j * np.pi * rng.random((nk, m)))[:, :, None]
+    _, _, ch2, _ = oracle.continuity(n, fac, ie, vertex, "s", ie, vec * ph, lam)
+    assert np.abs(ch1 - ch2).max() < 1e-12
+    assert np.abs(ch1[1:]).max() > 1e-3       # the sums are not trivially zero

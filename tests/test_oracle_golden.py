@@ -221,3 +221,18 @@ def test_oracle_matches_reference_driver_curve(oracle, golden):
     assert st == 0
     for k, ref in enumerate(driver_curve_reference(g)):
         assert np.abs(lam[k, :len(ref)] - ref).max() < 2e-6, (k, lam[k, :len(ref)], ref)
+
+
+def test_oracle_point_smoother_and_hiptmair_cycle(oracle, golden):
+    """The restated point smoother (gs*_simple_edge2d) and Hiptmair cycle
+    (hcycle_edge2d) against the reference's golden vectors."""
+    g = golden("hiptmair_n16.npz")
+    n0, L = int(g["n0"]), int(g["L"])
+    n = n0 << L
+    xf, yf = complex(g["xf"]), complex(g["yf"])
+    for d, name in ((0, "fwd"), (1, "bwd"), (2, "symm")):
+        got = oracle.gs_edge_simple(n, g["kappa"], xf, yf, 1.0, 1.0, d, g["b"], g["x"])
+        assert np.abs(got - g["simple_" + name]).max() < 1e-12 * np.abs(g["simple_" + name]).max()
+    for key, coarse, cycles in (("hcycle", 1, 2), ("hcycle_nocoarse", 0, 1)):
+        got = oracle.hcycle_edge(n0, L, g["kappa"], xf, yf, 2, coarse, cycles, g["b"], np.zeros_like(g["b"]))
+        assert np.abs(got - g[key]).max() < 1e-11 * np.abs(g[key]).max(), key
