@@ -329,6 +329,24 @@ int mxg_bloch_surface(mxg_solver *s, int steps, double *lambda, int *nsteps, dou
  * complex128 on the device; the decisions on the host. */
 int mxg_bloch_continuity(mxg_solver *s, int nk, const int *vertex, int continuity, int chern_vectors,
                          double *lambda, mxg_field *chern, int *sign);
+/* The protocol file of the reference's Bloch scan (exp_bloch2d.c:416-443
+ * header, 754-760 the starting point, 1227-1235 every later point): the
+ * header with the settings below, then per point its index, the m
+ * eigenvalues, block steps, seconds for the point and accumulated seconds,
+ * the real and imaginary part of each Chern partial sum and the swap count,
+ * formatted as the reference formats them.  steps, seconds and sign may be
+ * NULL (written as 0); chern (nk*chern_vectors) may be NULL when
+ * chern_vectors is 0. */
+typedef struct {
+  const char *pattern;   /* "Permittivity pattern" of the header */
+  int n0, L;             /* coarse grid intervals, refinement levels */
+  int chern_vectors;
+  int extrapolation;     /* 'n', '1', '2' */
+  int stopping;          /* 'r' residual, 'f' fixed steps */
+  int continuity;        /* 'n', 's', 'r' */
+} mxg_protocol_info;
+int mxg_write_protocol(const char *filename, const mxg_protocol_info *info, int nk, int m, const double *lambda,
+                       const int *steps, const double *seconds, const mxg_field *chern, const int *sign);
 /* eigenvectors of the last solved batch: wave k-points x m vectors in dense order */
 int mxg_solver_eigenvectors(const mxg_solver *s, mxg_field *host);
 /* device time of the last mxg_bloch_solve in milliseconds, and the number of

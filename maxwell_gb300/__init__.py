@@ -42,6 +42,26 @@ class SolveOpts(C.Structure):
                                                                                   ("refine", C.c_int)]
 
 
+class ProtocolInfo(C.Structure):
+    """mxg_protocol_info (the settings in the header of the reference's
+    protocol file, exp_bloch2d.c:416-443)."""
+    _fields_ = [("pattern", C.c_char_p), ("n0", C.c_int), ("L", C.c_int), ("chern_vectors", C.c_int),
+                ("extrapolation", C.c_int), ("stopping", C.c_int), ("continuity", C.c_int)]
+
+
+def write_protocol(filename, pattern, n0, L, lam, steps=None, seconds=None, chern=None, sign=None,
+                   extrapolation="2", stopping="r", continuity="s"):
+    """mxg_write_protocol: the reference's protocol file of a Bloch scan."""
+    lam = np.ascontiguousarray(lam, np.float64)
+    nk, m = lam.shape
+    cv = 0 if chern is None else np.asarray(chern).shape[1]
+    info = ProtocolInfo(pattern.encode(), n0, L, cv, ord(extrapolation), ord(stopping), ord(continuity))
+    arrs = [None if a is None else np.ascontiguousarray(a, t)
+            for a, t in ((steps, np.int32), (seconds, np.float64), (chern, np.complex128), (sign, np.int32))]
+    check(lib().mxg_write_protocol(filename.encode(), C.byref(info), nk, m, _ptr(lam),
+                                   *[None if a is None else _ptr(a) for a in arrs]), "mxg_write_protocol")
+
+
 class EpsPattern(C.Structure):
     """mxg_epspattern (the reference's epspattern, grid2d.h:40-62)."""
     _fields_ = [("rectangle", C.POINTER(C.c_double)), ("rectangles", C.c_int),
@@ -123,6 +143,7 @@ def lib() -> C.CDLL:
             "gsbackward_simple_edge2d_gpu": (I, [Field, Field, P, P]),
             "gssymm_simple_edge2d_gpu": (I, [Field, Field, P, P]),
             "hcycle_edge2d_gpu": (I, [I, I, P, P, P, P, P, P]),
+            "mxg_write_protocol": (I, [C.c_char_p, P, I, I, P, P, P, P, P]),
             "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
             "swap_edge2d_gpu": (I, [P, P]),

@@ -9,6 +9,7 @@
 
 #include <cuda_runtime_api.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1138,4 +1139,62 @@ int getkappa_grid2d_gpu(const grid2d_gpu *g, double *kappa)
 {
   memcpy(kappa, g->h_kappa, sizeof(double) * g->n * g->n);
   return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* protocol file of the Bloch scan (exp_bloch2d.c:416-443, 754-760,       */
+/* 1227-1235)                                                            */
+/* ------------------------------------------------------------------ */
+
+int mxg_write_protocol(const char *filename, const mxg_protocol_info *info, int nk, int m, const double *lambda,
+                       const int *steps, const double *seconds, const mxg_field *chern, const int *sign)
+{
+  FILE *out;
+  int l, i, cv;
+  double accum = 0.0;
+  if(!filename || !info || nk < 1 || m < 1 || !lambda || info->chern_vectors < 0 || (info->chern_vectors && !chern))
+    return MXG_EINVAL;
+  cv = info->chern_vectors;
+  out = fopen(filename, "w");
+  if(!out) return MXG_EINVAL;
+  fprintf(out,
+          "# Bloch eigenvalues\n"
+          "# ----------------------------------------\n"
+          "# Permittivity pattern: %s\n"
+          "# Coarse grid intervals: %d\n"
+          "# Refinement levels: %d\n"
+          "# Chern vectors: %d\n"
+          "# Extrapolation method: %s\n"
+          "# Stopping criterion: %s\n"
+          "# Eigenvector continuity: %s\n"
+          "# ----------------------------------------\n"
+          "# 1: Bloch step\n"
+          "# 2..%d: Eigenvalues\n"
+          "# %d: Iterations\n"
+          "# %d: Time for this step [s]\n"
+          "# %d: Total time to this step [s]\n"
+          "# %d: Chern partial integral, real part\n"
+          "# %d: Chern partial integral, imaginary part\n"
+          "# ----------------------------------------\n",
+          info->pattern ? info->pattern : "",
+          info->n0, info->L, cv,
+          info->extrapolation == '1' ? "1st order" : info->extrapolation == '2' ? "2nd order" : "None",
+          info->stopping == 'f' ? "Fixed steps" : "Residual",
+          info->continuity == 's' ? "Sign" : info->continuity == 'r' ? "Reorder" : "None",
+          m + 1, m + 2, m + 3, m + 4, m + 5, m + 6);
+  /* the starting point: its eigenvalues only */
+  fprintf(out, "0");
+  for(i = 0; i < m; i++) fprintf(out, " %f", lambda[i]);
+  fprintf(out, "\n");
+  for(l = 1; l < nk; l++) {
+    double t = seconds ? seconds[l] : 0.0;
+    accum += t;
+    fprintf(out, "%d", l);
+    for(i = 0; i < m; i++) fprintf(out, " %f", lambda[(size_t) l * m + i]);
+    fprintf(out, "  %d  %.1f %.1f ", steps ? steps[l] : 0, t, accum);
+    for(i = 0; i < cv; i++)
+      fprintf(out, " %f %f", creal(chern[(size_t) l * cv + i]), cimag(chern[(size_t) l * cv + i]));
+    fprintf(out, "  %d\n", sign ? sign[l] : 0);
+  }
+  return fclose(out) ? MXG_EINVAL : 0;
 }

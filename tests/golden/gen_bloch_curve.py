@@ -56,7 +56,10 @@ def main() -> None:
     eigs = IEIGS + THROWAWAY
     lam, iters, chern = [], [], []
     with open(os.path.join(RUN, "bloch2d.dat")) as f:
-        for line in f:
+        protocol = f.read().splitlines()
+    header = [line for line in protocol if line.startswith("#")]
+    if True:
+        for line in protocol:
             if line.startswith("#") or not line.strip():
                 continue
             v = line.split()
@@ -75,7 +78,7 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "bloch_curve_n16_kivshar.npz"),
                         n0=N0, L=LEVELS, disc=np.array(DISC), eps_base=1.0, ieigs=IEIGS, m=IEIGS + THROWAWAY,
                         tol=TOL, kpoints=ks, factors=fac, lam=np.array(lam), iterations=np.array(iters),
-                        chern=np.array(chern))
+                        chern=np.array(chern), protocol_header=np.array(header))
     print("points", npts, "lam", np.array(lam).shape)
 
 

@@ -94,3 +94,31 @@ def test_c_caller_example_compiles(built):
     r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-c", src, "-o", os.devnull,
                         "-I", os.path.join(root, "include")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_protocol_file_matches_the_reference_format(built, golden, tmp_path):
+    """mxg_write_protocol writes the header of the reference driver's
+    protocol file line for line (the header its own run wrote, kept in the
+    driver-curve fixture) and the per-point lines in its format: the values
+    read back as the driver's protocol is read.  Host code only."""
+    g = golden("bloch_curve_n16_kivshar.npz")
+    lam, chern = g["lam"], g["chern"]
+    nk, m = lam.shape
+    f = tmp_path / "bloch2d.dat"
+    mx.write_protocol(str(f), "Kivshar", int(g["n0"]), int(g["L"]), lam, steps=g["iterations"],
+                      seconds=np.full(nk, 0.25), chern=chern, sign=np.zeros(nk, np.int32),
+                      extrapolation="2", stopping="r", continuity="s")
+    lines = f.read_text().splitlines()
+    header = [ln for ln in lines if ln.startswith("#")]
+    assert header == list(g["protocol_header"])
+    rows = [ln.split() for ln in lines if not ln.startswith("#")]
+    assert len(rows) == nk and len(rows[0]) == 1 + m
+    for l, v in enumerate(rows):
+        assert int(v[0]) == l
+        assert np.allclose([float(x) for x in v[1:1 + m]], lam[l], atol=5e-7)
+        if l:
+            assert int(v[1 + m]) == int(g["iterations"][l])
+            assert float(v[3 + m]) == pytest.approx(0.25 * l, abs=0.06)   # printed with one decimal
+            c = [float(x) for x in v[4 + m:4 + m + 2 * chern.shape[1]]]
+            assert np.allclose(c[0::2], chern[l].real, atol=5e-7) and np.allclose(c[1::2], chern[l].imag, atol=5e-7)
+            assert int(v[-1]) == 0

@@ -141,3 +141,86 @@ def test_band_gap_objective_through_autograd():
         fm = objective(torch.from_numpy(solve(em)[:, :IEIGS])).item()
         fd = (fp - fm) / (2 * h)
         assert abs(fd - grad[c]) <= 1e-5 * np.abs(grad[cells]).max(), (c, fd, grad[c])
+
+
+def test_config4_band_gap_gradient_full_size(oracle):
+    """The differentiation configuration at its stated size: 128^2 cells,
+    eps = 1 + 11 sigmoid(g) from a seeded Gaussian random field of
+    correlation length 0.1, 24 k-points on Gamma-X-M-Gamma, objective
+    softmin_k lambda_9 - softmax_k lambda_8 (temperature 1e-3), gradient on
+    all 16,384 cells from the adjoint reduction (FP64 GPU solver).
+    (1) Against the FP64 CPU reference gradient: the oracle's reduction on the
+    oracle's own eigenvectors, 1e-8.  (2) Against central finite differences
+    with step 1e-6 (relative to eps_c) on 64 cells drawn at random among
+    those whose gradient is at least a tenth of the largest, 1e-5.  The
+    objective's weights exp(-(lambda - extremum) / T) of all but the extremal
+    k-points are below 1e-12 here (asserted), so the finite-difference and
+    CPU solves take only the k-points above that weight; the others move the
+    objective by less than 1e-12 h."""
+    n0, L, ie, m, T = 8, 4, 10, 12, 1e-3
+    n = n0 << L
+    rng = np.random.default_rng(17)
+    w = rng.standard_normal((n, n))
+    f = np.fft.fftfreq(n)[:, None] ** 2 + np.fft.fftfreq(n)[None, :] ** 2
+    g = np.real(np.fft.ifft2(np.fft.fft2(w) * np.exp(-0.5 * (2 * np.pi * 0.1 * n) ** 2 * f)))
+    g = (g - g.mean()) / g.std()
+    eps = 1.0 + 11.0 / (1.0 + np.exp(-g.reshape(-1)))
+    seg = [np.pi, np.pi, np.pi * np.sqrt(2.0)]
+    pts = []
+    for t in np.linspace(0.0, sum(seg), 24):
+        if t <= seg[0]:
+            pts.append((t, 0.0))
+        elif t <= seg[0] + seg[1]:
+            pts.append((np.pi, t - seg[0]))
+        else:
+            s_ = (t - seg[0] - seg[1]) / np.sqrt(2.0)
+            pts.append((np.pi - s_, np.pi - s_))
+    fac = np.exp(1j * np.array(pts))
+
+    def gpu_solve(e, f_, vectors=False):
+        s = mx.Solver(1.0 / e, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=0, wave=len(f_), relative=1,
+                      tol=1e-11, max_nested=60, max_steps=120)
+        lam, steps, res = s.solve(f_)
+        assert res[:, :ie].max() <= 1e-11
+        return (lam, s.eigenvectors()) if vectors else lam
+
+    lam, vec = gpu_solve(eps, fac, True)
+    wmin = np.exp(-(lam[:, 9] - lam[:, 9].min()) / T)
+    wmax = np.exp((lam[:, 8] - lam[:, 8].max()) / T)
+    wmin, wmax = wmin / wmin.sum(), wmax / wmax.sum()
+    # d objective / d lambda: softmin weights on band 9, -softmax weights on band 8
+    W = np.zeros((len(fac), m))
+    W[:, 9], W[:, 8] = wmin, -wmax
+    W = cluster_average(lam[:, :m], W)
+    grad = mx.eps_sensitivity(n, 1.0 / eps, fac, vec, W)
+    active = np.nonzero((wmin > 1e-12) | (wmax > 1e-12))[0]
+    assert len(active) < len(fac)
+    # (1) the CPU FP64 reference gradient on the active k-points
+    want = np.zeros(n * n)
+    for k in active:
+        st, lam_o, _, _, vec_o = oracle.bloch_solve(1.0 / eps, fac[k:k + 1], n0=n0, L=L, ieigs=ie, m=m, method=1,
+                                                    max_nested=60, max_steps=120, tol=1e-11, relative=1,
+                                                    extrapolation="n", wave=1, want_vectors=True)
+        assert st == 0
+        wk = np.zeros((1, m))
+        wk[0, 9], wk[0, 8] = wmin[k], -wmax[k]
+        want += oracle.eps_sensitivity(n, 1.0 / eps, *fac[k], vec_o[0], cluster_average(lam_o[:, :m], wk)[0])
+    assert np.abs(grad - want).max() / np.abs(want).max() < 1e-8
+
+    # (2) central differences of the objective on 64 cells
+    def objective(lam_active):
+        full = lam.copy()
+        full[active] = lam_active
+        return (-T * np.log(np.exp(-(full[:, 9] - full[:, 9].min()) / T).sum()) + full[:, 9].min()
+                - T * np.log(np.exp((full[:, 8] - full[:, 8].max()) / T).sum()) - full[:, 8].max())
+
+    big = np.nonzero(np.abs(grad) >= 0.1 * np.abs(grad).max())[0]
+    cells = rng.choice(big, min(64, len(big)), replace=False)
+    fd = np.zeros(len(cells))
+    for q, c in enumerate(cells):
+        h = 1e-6 * eps[c]
+        ep, em = eps.copy(), eps.copy()
+        ep[c] += h
+        em[c] -= h
+        fd[q] = (objective(gpu_solve(ep, fac[active])) - objective(gpu_solve(em, fac[active]))) / (2 * h)
+    assert np.abs(fd - grad[cells]).max() / np.abs(grad[cells]).max() < 1e-5, (fd, grad[cells])
