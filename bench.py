@@ -478,7 +478,7 @@ def run_surface(args):
     precision, relative residual 1e-8.  Not the headline metric: one JSON
     line of k-points/s."""
     import maxwell_gb300 as mx
-    n0, L, steps, wave = 8, 5, 32, 64
+    n0, L, steps, wave = 8, 5, 32, args.wave
     n = n0 << L
     h = 1.0 / n
     i = np.arange(n)
@@ -489,21 +489,22 @@ def run_surface(args):
             inside |= (X - cx) ** 2 + (Y - cy) ** 2 <= 0.15 ** 2
     kap = np.ascontiguousarray(np.where(inside, 1.0 / 10.0, 1.0).reshape(-1))
     s = mx.Solver(kap, n0=n0, L=L, ieigs=IEIGS, m=BLOCK, method=1, precision=1, max_nested=MAX_NESTED,
-                  max_steps=60, wave=wave, relative=1, tol=TOL, extrapolation="2")
+                  max_steps=60, wave=wave, relative=1, tol=TOL, extrapolation=args.extrapolation)
     for _ in range(args.warmup):
         s.solve(factors_of(gamma_x_m_gamma(wave)))
     t0 = time.time()
     lam, st, res = s.surface(steps)
     wall = time.time() - t0
     ms, nl = s.stats()
-    print(json.dumps({"metric": "k-points/s, full-zone surface 256^2, 32x32 k-grid in waves of 64",
+    print(json.dumps({"metric": f"k-points/s, full-zone surface 256^2, 32x32 k-grid in waves of {wave}",
                       "value": steps * steps / (ms / 1e3), "unit": "k-points/s", "wall_s": wall,
                       "steps_first_wave": float(st.reshape(-1)[:wave].mean()),
                       "steps_later_waves": float(st.reshape(-1)[wave:].mean()),
                       "max_rel_residual": float(res[..., :IEIGS].max()), "gpu_launches": nl,
                       "cold_restarts": s.restarts(),
-                      "config": {"workload": "256^2, 4 discs eps=10 r=0.15, 32x32 k-grid over the zone, "
-                                             "waves of 64, 12 pairs block 16, LOBPCG, relative residual 1e-8"}}),
+                      "config": {"workload": f"256^2, 4 discs eps=10 r=0.15, 32x32 k-grid over the zone, "
+                                             f"waves of {wave}, extrapolation '{args.extrapolation}', 12 pairs "
+                                             "block 16, LOBPCG, relative residual 1e-8"}}),
           flush=True)
 
 
@@ -519,6 +520,9 @@ def main():
     ap.add_argument("--reps", type=int, default=5, help="timed calls per kernel of the --kernels table")
     ap.add_argument("--surface", action="store_true", help="the full-zone surface workload instead of the metric")
     ap.add_argument("--config5", action="store_true", help="the 2048^2 block-32 workload instead of the metric")
+    ap.add_argument("--wave", type=int, default=64, help="k-points per wave of the --surface workload")
+    ap.add_argument("--extrapolation", default="2", choices=["n", "1", "2"],
+                    help="warm start of the --surface workload's later waves")
     args = ap.parse_args()
     if args.kernels:
         run_kernels(args)

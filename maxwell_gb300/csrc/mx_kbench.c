@@ -60,7 +60,8 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
   float *kf = 0, *kdd = 0, *hkf = 0, *hkdd = 0;
   void *afw = 0, *E = 0, *X = 0, *P = 0, *r = 0, *b = 0, *x = 0, *d = 0, *bc = 0, *nb = 0, *nx = 0, *nd = 0,
        *nbc = 0, *out = 0, *cw = 0;
-  int *gamma = 0, *hg = 0;
+  int *gamma = 0, *hg = 0, *sel = 0, *info = 0;
+  double *rwork = 0;
   cudaStream_t st = 0;
   cudaEvent_t e0 = 0, e1 = 0;
   size_t gbytes;
@@ -106,7 +107,9 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
      || cudaMalloc(&E, E8 * 16) || cudaMalloc(&out, E8 * 16) || cudaMalloc(&X, E8 * 8) || cudaMalloc(&P, E8 * 8)
      || cudaMalloc(&r, E8 * 8) || cudaMalloc(&b, E8 * 8) || cudaMalloc(&x, E8 * 8) || cudaMalloc(&d, E8 * 8)
      || cudaMalloc(&bc, E8 / 4 * 8) || cudaMalloc(&nb, V8 * 8) || cudaMalloc(&nx, V8 * 8) || cudaMalloc(&nd, V8 * 8)
-     || cudaMalloc(&nbc, V8 / 4 * 8))
+     || cudaMalloc(&nbc, V8 / 4 * 8) || cudaMalloc((void **) &sel, sizeof(int) * 3 * m * K)
+     || cudaMalloc((void **) &info, sizeof(int) * K)
+     || cudaMalloc((void **) &rwork, sizeof(double) * mxk_ritz_work_doubles(3 * m) * K))
     { err = MXG_ENOMEM; goto done; }
   TRY((int) cudaMemcpy(kd, hk, sizeof(double) * nn, cudaMemcpyHostToDevice));
   TRY((int) cudaMemcpy(kf, hkf, sizeof(float) * nn, cudaMemcpyHostToDevice));
@@ -194,6 +197,18 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
          mxk_center(n, m, K, gamma, MX_CDD, E, acc, st));
     TIME("axpy_c64_into_cdd", E8 * (s8 + 2 * s16), 1,
          mxk_axpy(-1e-3, 0.0, MX_C64, x, MX_CDD, E, E8, st));
+    /* the Ritz step on the Gram matrices of the block_gram row (every
+     * column selected); its bytes are the two 48 x 48 matrices per k-point */
+    {
+      int *hs = malloc(sizeof(int) * 3 * m * K), q;
+      if(!hs) { err = MXG_ENOMEM; goto done; }
+      for(q = 0; q < 3 * m * K; q++) hs[q] = 1;
+      err = (int) cudaMemcpy(sel, hs, sizeof(int) * 3 * m * K, cudaMemcpyHostToDevice);
+      free(hs);
+      if(err) goto done;
+    }
+    TIME("rayleigh_ritz_48", 2.0 * 16.0 * 9 * m * m * K, 1,
+         mxk_rayleigh_ritz(3 * m, m, K, ga, gm, sel, 1e-6, -1e300, coef, theta, info, rwork, st));
   }
 #undef TIME
 
@@ -202,6 +217,7 @@ done:
   cudaFree(theta); cudaFree(ga); cudaFree(gm); cudaFree(coef); cudaFree(cw); cudaFree(stats); cudaFree(acc);
   cudaFree(gs); cudaFree(E); cudaFree(out); cudaFree(X); cudaFree(P); cudaFree(r); cudaFree(b); cudaFree(x);
   cudaFree(d); cudaFree(bc); cudaFree(nb); cudaFree(nx); cudaFree(nd); cudaFree(nbc);
+  cudaFree(sel); cudaFree(info); cudaFree(rwork);
   free(hk); free(hkf); free(hkdd); free(h_ph); free(hmu); free(hg);
   if(e0) cudaEventDestroy(e0);
   if(e1) cudaEventDestroy(e1);
