@@ -1064,6 +1064,38 @@ extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, 
   return 0;
 }
 
+// ------------------------------------------------------------------
+// column selection of the Ritz basis from the residual statistics: column
+// i of block j of k-point k stays when j == 0 (the eigenvector block), when
+// every column is wanted, or while residual i of k has not met the
+// tolerance (soft locking), the residual norm formed as the host forms it
+// from the same statistics
+// ------------------------------------------------------------------
+namespace {
+__global__ void k_select_columns(int ns, int m, int K, const double* __restrict__ stats,
+                                 const double* __restrict__ mu, double tol, int relative, int all, int* sel) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns * K) return;
+  int k = t / ns, c = t % ns, j = c / m, i = c % m;
+  int keep = 1;
+  if (j != 0 && !all) {
+    const double* st = stats + ((size_t) k * m + i) * 5;
+    double r = sqrt(st[0] > 0.0 ? st[0] : 0.0);
+    if (relative) r /= fabs(mu[(size_t) k * m + i]) * sqrt(st[1]) + 1e-300;
+    keep = !(r <= tol);
+  }
+  sel[t] = keep;
+}
+}  // namespace
+
+extern "C" int mxk_select_columns(int ns, int m, int K, const double* stats, const double* mu, double tol,
+                                  int relative, int all, int* sel, mx_stream s) {
+  k_select_columns<<<(ns * K + 255) / 256, 256, 0, (cudaStream_t) s>>>(ns, m, K, stats, mu, tol, relative, all,
+                                                                      sel);
+  MX_CHECK_LAUNCH();
+  return 0;
+}
+
 extern "C" int mxk_eps_sensitivity(int n, int m, int K, const double* ph, const double* kappa, const double* w,
                                    int pe, const void* e, double* grad, mx_stream s) {
   size_t nc = (size_t) n * n;

@@ -171,6 +171,11 @@ int mxk_block_gram(int n, int m, int K, const double *phases, mxk_kappa kap, int
 int mxk_block_combine(int n, int m, int K, int nb, const int *precs, const void *const *ptrs,
                       const double *coef, int ldc, int row0, void *cwork, int prec_out, void *out,
                       mx_stream s);
+/* sel[k*ns + j*m + i] = j == 0 || all || residual i of k (from the
+ * statistics of mxk_block_residual: absolute, or relative to |mu| ||M e||)
+ * above tol: the columns of the Ritz basis under soft locking */
+int mxk_select_columns(int ns, int m, int K, const double *stats, const double *mu, double tol,
+                       int relative, int all, int *sel, mx_stream s);
 /* per-cell eigenvalue sensitivity: grad[c] = -n^2 kappa_c^2 sum_{k,v} w[k*m+v] |curl_c e|^2 */
 int mxk_eps_sensitivity(int n, int m, int K, const double *phases, const double *kappa,
                         const double *weights, int prec_e, const void *e, double *grad,

@@ -94,6 +94,18 @@ struct mxg_solver {
    * V-cycles of the preconditioner and the node V-cycles of a lifting */
   cudaGraphExec_t gpre[MAXL], glift[MAXL];
   long gpre_n[MAXL], glift_n[MAXL];   /* kernel launches each graph holds */
+  /* the Ritz step (Gram, column selection, Rayleigh-Ritz, combinations) per
+   * level, block count and which buffers E and P sit in */
+  cudaGraphExec_t gritz[MAXL][3][2][2];
+  long gritz_n[MAXL][3][2][2];
+  void *E0, *P0;                       /* the first buffers of E and P */
+  struct {
+    int nb, with_p;
+    int pr[3];
+    const void *pp[3];
+    double drop, theta_min;
+  } rb;                                /* arguments of the Ritz step being run */
+  int ritz_pending;                    /* a Ritz step's info and Ritz values not yet read */
   int graphs;                          /* 1 capture and replay, 0 launch directly */
   int restarts;                       /* warm-started waves solved again cold */
   int debug;                          /* per-step residual trace on stderr */
@@ -126,8 +138,13 @@ void mxg_solver_free(mxg_solver *s)
   int l;
   if(!s) return;
   for(l = 0; l <= s->L; l++) {
+    int a, b, c;
     if(s->gpre[l]) cudaGraphExecDestroy(s->gpre[l]);
     if(s->glift[l]) cudaGraphExecDestroy(s->glift[l]);
+    for(a = 0; a < 3; a++)
+      for(b = 0; b < 2; b++)
+        for(c = 0; c < 2; c++)
+          if(s->gritz[l][a][b][c]) cudaGraphExecDestroy(s->gritz[l][a][b][c]);
     cudaFree(s->kd[l]); cudaFree(s->kf[l]); cudaFree(s->kdd[l]); cudaFree(s->kafw[l]);
     cudaFree(s->b[l]); cudaFree(s->x[l]); cudaFree(s->d[l]);
     cudaFree(s->bg[l]); cudaFree(s->xg[l]); cudaFree(s->dg[l]);
@@ -246,6 +263,8 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
      || dalloc((void **) &s->cacc, sizeof(double) * 4 * K * m)
      || dalloc(&s->combw, (size_t) 16 * ns * m * K))
     goto fail;
+  s->E0 = s->E;
+  s->P0 = s->P;
   s->gscratch_bytes = (size_t) K * 256 * (ns * (ns + 1) / 2) * 4 * sizeof(double);
   if(s->gscratch_bytes > ((size_t) 1 << 30)) s->gscratch_bytes = (size_t) 1 << 30;
   if(dalloc((void **) &s->gscratch, s->gscratch_bytes)) goto fail;
@@ -544,7 +563,18 @@ static int residual(mxg_solver *s, int l, int write_rhs)
   L_(mxk_block_residual(s->n[l], m, K, s->ph, kap(s, l), s->mu, s->pe, s->E, s->pg,
                         write_rhs ? s->b[l] : 0, s->stats, s->st));
   TRY((int) cudaMemcpyAsync(s->h_stats, s->stats, sizeof(double) * NSTAT * m * K, cudaMemcpyDeviceToHost, s->st));
+  if(s->ritz_pending) {
+    /* the Ritz step before this residual: its status and Ritz values (the
+     * shifts mu the residual was formed with) come back with the statistics */
+    TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * K, cudaMemcpyDeviceToHost, s->st));
+    TRY((int) cudaMemcpyAsync(s->h_mu, s->mu, sizeof(double) * m * K, cudaMemcpyDeviceToHost, s->st));
+  }
   TRY((int) cudaStreamSynchronize(s->st));
+  if(s->ritz_pending) {
+    s->ritz_pending = 0;
+    for(k = 0; k < K; k++)
+      if(s->h_info[k] < m) return MXG_ECONV;
+  }
   for(k = 0; k < K; k++)
     for(i = 0; i < m; i++) {
       const double *st = s->h_stats + ((size_t) k * m + i) * NSTAT;
@@ -578,12 +608,16 @@ static void swapp(void **a, void **b)
   *b = t;
 }
 
-/* Rayleigh-Ritz on the nb blocks (precisions pr, pointers pp) -> coef, theta
- * with soft locking of converged columns; writes the new E (and P) */
-static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop,
-                double theta_min)
+/* The launches of one Ritz step on the blocks of s->rb: Gram matrices,
+ * column selection from the last residual statistics (soft locking),
+ * Rayleigh-Ritz by Cholesky-QR and Jacobi, the Ritz values as the next
+ * shifts mu, and the combinations into En (and Pn).  No host decision sits
+ * between them, so the sequence is captured as one CUDA graph. */
+static int ritz_body(mxg_solver *s, int l)
 {
-  int m = s->m, K = s->K, ns = nb * m, k, i, j;
+  const int nb = s->rb.nb, m = s->m, K = s->K, ns = nb * m;
+  const int *pr = s->rb.pr;
+  const void *const *pp = s->rb.pp;
   /* the residual of E sits in b[l] (written by residual()) with the Ritz
    * values mu; the mixed solver forms the E-to-search-block entries from it */
   const void *rr = (s->pe == MX_CDD && nb > 1) ? s->b[l] : 0;
@@ -596,26 +630,41 @@ static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *
                     s->gscratch_bytes, s->st));
   s->launches++;   /* the reduction of the partial sums */
   prof_end(s, on);
-  for(k = 0; k < K; k++)
-    for(j = 0; j < nb; j++)
-      for(i = 0; i < m; i++)
-        s->h_sel[k * ns + j * m + i] = j == 0 || s->all_columns || !(s->h_res[k * m + i] <= s->o.tol);
-  TRY((int) cudaMemcpyAsync(s->sel, s->h_sel, sizeof(int) * ns * K, cudaMemcpyHostToDevice, s->st));
+  L_(mxk_select_columns(ns, m, K, s->stats, s->mu, s->o.tol, s->o.relative, s->all_columns, s->sel, s->st));
   if(tm) cudaEventRecord(s->tev[PH_RR], s->st);
-  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, drop, theta_min, s->coef, s->theta, s->info, s->rwork,
-                       s->st));
-  TRY((int) cudaMemcpyAsync(s->h_info, s->info, sizeof(int) * K, cudaMemcpyDeviceToHost, s->st));
-  TRY((int) cudaMemcpyAsync(s->h_mu, s->theta, sizeof(double) * m * K, cudaMemcpyDeviceToHost, s->st));
-  TRY((int) cudaStreamSynchronize(s->st));
-  for(k = 0; k < K; k++)
-    if(s->h_info[k] < m) return MXG_ECONV;
+  L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, s->rb.drop, s->rb.theta_min, s->coef, s->theta, s->info,
+                       s->rwork, s->st));
+  TRY((int) cudaMemcpyAsync(s->mu, s->theta, sizeof(double) * m * K, cudaMemcpyDeviceToDevice, s->st));
   if(tm) cudaEventRecord(s->tev[PH_COMB], s->st);
-  if(with_p)
+  if(s->rb.with_p)
     L_(mxk_block_combine(s->n[l], m, K, nb - 1, pr + 1, pp + 1, s->coef, ns, m, s->combw, s->pg, s->Pn, s->st));
   L_(mxk_block_combine(s->n[l], m, K, nb, pr, pp, s->coef, ns, 0, s->combw, s->pe, s->En, s->st));
+  return 0;
+}
+
+/* Rayleigh-Ritz on the nb blocks (precisions pr, pointers pp) -> coef, theta
+ * with soft locking of converged columns; writes the new E (and P).  The
+ * step's status (a rank-deficient basis) and its Ritz values reach the host
+ * with the next residual(). */
+static int ritz(mxg_solver *s, int l, int nb, const int *pr, const void *const *pp, int with_p, double drop,
+                double theta_min)
+{
+  int q;
+  s->rb.nb = nb;
+  s->rb.with_p = with_p;
+  for(q = 0; q < nb; q++) { s->rb.pr[q] = pr[q]; s->rb.pp[q] = pp[q]; }
+  s->rb.drop = drop;
+  s->rb.theta_min = theta_min;
+  if(s->timing || s->all_columns)
+    TRY(ritz_body(s, l));
+  else {
+    int pe = s->E != s->E0, pq = s->P != s->P0;
+    TRY(run_graphed(s, l, &s->gritz[l][nb - 1][pe][pq], &s->gritz_n[l][nb - 1][pe][pq], ritz_body));
+  }
+  s->ritz_pending = 1;
   swapp(&s->E, &s->En);
   if(with_p) swapp(&s->P, &s->Pn);
-  return upload_mu(s);
+  return 0;
 }
 
 /* pivot^2 below which Cholesky-QR drops a column of the Ritz basis
