@@ -249,6 +249,8 @@ def run_ours(args):
         return mx.Solver(kap, n0=N0, L=LEVELS, ieigs=IEIGS, m=BLOCK, method=1, precision=precision,
                          max_nested=MAX_NESTED, max_steps=60, wave=wave, relative=1, tol=TOL)
 
+    if args.autotune:
+        mx.autotune(n, NK, BLOCK, 3)
     s = make(1, NK)
     for _ in range(args.warmup):
         s.solve(fac)
@@ -340,7 +342,8 @@ def run_ours(args):
         "config": {"workload": "512^2 disc eps=12 r=0.3, 32 k-points Gamma-X-M-Gamma, 12 pairs block 16, "
                                "LOBPCG, 7 MG levels FP32, relative residual 1e-8",
                    "k_points_per_gpu": NK, "grid": n, "pairs": IEIGS, "block": BLOCK, "levels": LEVELS + 1,
-                   "l2": "working set (> 10 GB per step) far above the 129 MB L2", "device": dev},
+                   "l2": "working set (> 10 GB per step) far above the 129 MB L2", "device": dev,
+                   "launch_shapes": dict(mx.get_tuning(), autotuned=bool(args.autotune))},
         "e2e": {"value": NK * ws * e2e_steps / e2e_t, "unit": "k-points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -523,6 +526,8 @@ def main():
     ap.add_argument("--wave", type=int, default=64, help="k-points per wave of the --surface workload")
     ap.add_argument("--extrapolation", default="2", choices=["n", "1", "2"],
                     help="warm start of the --surface workload's later waves")
+    ap.add_argument("--autotune", action="store_true",
+                    help="choose the block kernels' launch shapes on the workload's sizes before warm-up")
     args = ap.parse_args()
     if args.kernels:
         run_kernels(args)

@@ -144,6 +144,9 @@ def lib() -> C.CDLL:
             "gssymm_simple_edge2d_gpu": (I, [Field, Field, P, P]),
             "hcycle_edge2d_gpu": (I, [I, I, P, P, P, P, P, P]),
             "mxg_write_protocol": (I, [C.c_char_p, P, I, I, P, P, P, P, P]),
+            "mxg_get_tuning": (I, [P]),
+            "mxg_set_tuning": (I, [P]),
+            "mxg_autotune": (I, [I, I, I, I, P]),
             "mxg_bloch_surface": (I, [P, I, P, P, P]),
             "mxg_kernel_bench": (I, [I, I, I, I, P, I]),
             "swap_edge2d_gpu": (I, [P, P]),
@@ -202,6 +205,31 @@ def kernel_bench(n: int, K: int, m: int, reps: int = 5) -> list[dict]:
         raise RuntimeError(f"mxg_kernel_bench failed: {r}")
     return [{"name": rows[i].name.decode(), "ms": rows[i].ms, "bytes": rows[i].bytes,
              "launches": rows[i].launches} for i in range(r)]
+
+
+class Tuning(C.Structure):
+    """mxg_tuning: launch shapes of the block kernels."""
+    _fields_ = [("gram_waves", C.c_int), ("combine_ctas", C.c_int), ("residual_sites", C.c_int)]
+
+
+def autotune(n: int, K: int, m: int, reps: int = 3) -> dict:
+    """mxg_autotune: choose the launch shapes for n x n cells, K k-points,
+    block m, and keep them for this process."""
+    t = Tuning()
+    r = lib().mxg_autotune(n, K, m, reps, C.byref(t))
+    if r != 0:
+        raise RuntimeError(f"mxg_autotune failed: {r}")
+    return {"gram_waves": t.gram_waves, "combine_ctas": t.combine_ctas, "residual_sites": t.residual_sites}
+
+
+def get_tuning() -> dict:
+    t = Tuning()
+    check(lib().mxg_get_tuning(C.byref(t)), "mxg_get_tuning")
+    return {"gram_waves": t.gram_waves, "combine_ctas": t.combine_ctas, "residual_sites": t.residual_sites}
+
+
+def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int) -> None:
+    check(lib().mxg_set_tuning(C.byref(Tuning(gram_waves, combine_ctas, residual_sites))), "mxg_set_tuning")
 
 
 def header_functions() -> list[str]:

@@ -20,6 +20,34 @@
 
 using namespace mx;
 
+// ------------------------------------------------------------------
+// launch shapes that mxg_autotune chooses (process-wide; the defaults are
+// the shapes measured best on the 512^2, 32-k-point, block-16 workload)
+// ------------------------------------------------------------------
+static mxk_tuning g_tuning = {4, 2, 32};
+static int g_sms = 0;
+
+static int sm_count() {
+  if (!g_sms) {
+    int dev = 0, c = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && c > 0)
+      g_sms = c;
+    else
+      g_sms = 152;
+  }
+  return g_sms;
+}
+
+extern "C" void mxk_get_tuning(mxk_tuning* t) { *t = g_tuning; }
+extern "C" int mxk_set_tuning(const mxk_tuning* t) {
+  if (t->gram_waves < 1 || t->gram_waves > 64 || t->combine_ctas < 1 || t->combine_ctas > 16 ||
+      t->residual_sites < 1 || t->residual_sites > 1024)
+    return (int) cudaErrorInvalidValue;
+  g_tuning = *t;
+  return 0;
+}
+
 namespace {
 
 
@@ -661,9 +689,10 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
   int rows = 256 / m;
   if (m > 32) return (int) cudaErrorInvalidValue;
   size_t nsite = (size_t) n * n;
-  // about 32 sites per thread, so that the per-thread double reduction at
-  // the end stays small against the sweep
-  unsigned G = (unsigned) ((nsite + (size_t) rows * 32 - 1) / ((size_t) rows * 32));
+  // about residual_sites sites per thread, so that the per-thread double
+  // reduction at the end stays small against the sweep
+  const size_t per = (size_t) rows * g_tuning.residual_sites;
+  unsigned G = (unsigned) ((nsite + per - 1) / per);
   if (G < 1) G = 1;
   if (G > 4096) G = 4096;
   dim3 g(G, K), b(256);
@@ -938,7 +967,7 @@ static size_t gram_mixed_smem(int ns, int m) {
 }
 
 static int gram_chunks(int K, size_t nsite) {
-  int c = (4 * 152 + K - 1) / K;
+  int c = (g_tuning.gram_waves * sm_count() + K - 1) / K;
   if (c < 8) c = 8;
   if (c > 256) c = 256;
   size_t maxc = (nsite + TS - 1) / TS;
@@ -1024,9 +1053,9 @@ extern "C" int mxk_block_combine(int n, int m, int K, int nb, const int* precs, 
   for (int q = 0; q < nb; q++) aligned = aligned && ((uintptr_t) ptrs[q] & 15) == 0;
   if (m <= 16 && nfloat <= 2 && first_ok && rest64 && aligned &&
       (pout == MX_CDD || (pout == MX_C64 && precs[0] == MX_C64))) {
-    // one wave of CTAs, two per SM (152 SMs), each walking tiles of its k-point
+    // one wave of CTAs, combine_ctas per SM, each walking tiles of its k-point
     size_t ntiles = (2 * (size_t) n * n + CTE - 1) / CTE;
-    size_t want = (size_t) (2 * 152) / (size_t) K;
+    size_t want = (size_t) g_tuning.combine_ctas * sm_count() / (size_t) K;
     if (want < 1) want = 1;
     unsigned gx = (unsigned) (ntiles < want ? ntiles : want);
     dim3 g2(gx, K);

@@ -15,6 +15,15 @@ typedef struct CUstream_st *mx_stream;
 
 enum { MX_C64 = 0, MX_C128 = 1, MX_CDD = 2 };
 
+/* launch shapes of the block kernels: Gram CTAs per k-point =
+ * gram_waves * SMs / K, tiled-combination CTAs = combine_ctas * SMs, block
+ * residual sites per thread (mxg_autotune chooses them) */
+typedef struct {
+  int gram_waves, combine_ctas, residual_sites;
+} mxk_tuning;
+void mxk_get_tuning(mxk_tuning *t);
+int mxk_set_tuning(const mxk_tuning *t);
+
 /* sizes of one complex entry */
 size_t mxk_elem_size(int prec);
 

@@ -50,7 +50,46 @@ static void row(mxg_kbench_row *r, const char *name, float ms, int reps, double 
   r->launches = launches;
 }
 
+static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows, mxg_tuning *tune);
+
 int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows)
+{
+  if(!rows || maxrows < 16) return MXG_EINVAL;
+  return run(n, K, m, reps, rows, maxrows, 0);
+}
+
+int mxg_get_tuning(mxg_tuning *t)
+{
+  mxk_tuning q;
+  mxk_get_tuning(&q);
+  t->gram_waves = q.gram_waves;
+  t->combine_ctas = q.combine_ctas;
+  t->residual_sites = q.residual_sites;
+  return 0;
+}
+
+int mxg_set_tuning(const mxg_tuning *t)
+{
+  mxk_tuning q;
+  q.gram_waves = t->gram_waves;
+  q.combine_ctas = t->combine_ctas;
+  q.residual_sites = t->residual_sites;
+  return mxk_set_tuning(&q) ? MXG_EINVAL : 0;
+}
+
+int mxg_autotune(int n, int K, int m, int reps, mxg_tuning *chosen)
+{
+  mxg_tuning t;
+  int e;
+  if(!chosen) return MXG_EINVAL;
+  e = run(n, K, m, reps, 0, 0, &t);
+  if(e < 0) return e;
+  *chosen = t;
+  return mxg_set_tuning(&t);
+}
+
+/* the kernel table (rows) or, with tune, the search over launch shapes */
+static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows, mxg_tuning *tune)
 {
   size_t nn = (size_t) n * n, ne = 2 * nn, q;
   size_t E8 = ne * m * K, V8 = nn * m * K;       /* entries per edge / node block */
@@ -68,7 +107,7 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
   float ms;
   mxk_kappa kap;
 
-  if(n < 8 || (n & 1) || K < 1 || m < 1 || m > 16 || reps < 1 || !rows || maxrows < 16) return MXG_EINVAL;
+  if(n < 8 || (n & 1) || K < 1 || m < 1 || m > 16 || reps < 1) return MXG_EINVAL;
   lcg_state = 12345;
   if(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) || cudaEventCreate(&e0) || cudaEventCreate(&e1))
     { err = MXG_ENOMEM; goto done; }
@@ -155,6 +194,49 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
     if(nr < maxrows) row(rows + nr++, NAME, ms, reps, (double) (BYTES), LAUNCHES); \
   } while(0)
 
+  if(tune) {
+    /* each tunable in turn, the others at their current values: the
+     * candidate with the least time for `reps` calls wins */
+    static const int gw[] = {1, 2, 4, 8, 16}, cc[] = {1, 2, 3, 4}, rs[] = {8, 16, 32, 64, 128};
+    int pr3[3] = {MX_CDD, MX_C64, MX_C64};
+    const void *pp3[3];
+    mxk_tuning base, tr;
+    float best;
+    int c;
+    pp3[0] = E; pp3[1] = X; pp3[2] = P;
+    mxk_get_tuning(&base);
+#define TUNE(FIELD, LIST, CALL)                                                      \
+    do {                                                                             \
+      int bestv = base.FIELD;                                                        \
+      best = 1e30f;                                                                  \
+      for(c = 0; c < (int) (sizeof(LIST) / sizeof(LIST[0])); c++) {                 \
+        tr = base;                                                                   \
+        tr.FIELD = LIST[c];                                                          \
+        TRY(mxk_set_tuning(&tr));                                                    \
+        TRY(CALL);                                                                   \
+        TRY((int) cudaEventRecord(e0, st));                                          \
+        for(it = 0; it < reps; it++) TRY(CALL);                                      \
+        TRY((int) cudaEventRecord(e1, st));                                          \
+        TRY((int) cudaEventSynchronize(e1));                                         \
+        TRY((int) cudaEventElapsedTime(&ms, e0, e1));                                \
+        if(ms < best) { best = ms; bestv = LIST[c]; }                                \
+      }                                                                              \
+      base.FIELD = bestv;                                                            \
+      TRY(mxk_set_tuning(&base));                                                    \
+    } while(0)
+    TUNE(gram_waves, gw,
+         mxk_block_gram(n, m, K, ph, kap, 3, pr3, pp3, r, theta, ga, gm, gs, gbytes, st));
+    TUNE(combine_ctas, cc,
+         mxk_block_combine(n, m, K, 3, pr3, pp3, coef, 3 * m, 0, cw, MX_CDD, out, st));
+    TUNE(residual_sites, rs,
+         (cudaMemsetAsync(stats, 0, sizeof(double) * 5 * m * K, st),
+          mxk_block_residual(n, m, K, ph, kap, mu, MX_CDD, E, MX_C64, r, stats, st)));
+#undef TUNE
+    tune->gram_waves = base.gram_waves;
+    tune->combine_ctas = base.combine_ctas;
+    tune->residual_sites = base.residual_sites;
+    goto done;
+  }
   {
     const double s8 = 8.0, s16 = 16.0;
     const double kb4 = 4.0 * nn;

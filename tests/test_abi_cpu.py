@@ -122,3 +122,20 @@ def test_protocol_file_matches_the_reference_format(built, golden, tmp_path):
             c = [float(x) for x in v[4 + m:4 + m + 2 * chern.shape[1]]]
             assert np.allclose(c[0::2], chern[l].real, atol=5e-7) and np.allclose(c[1::2], chern[l].imag, atol=5e-7)
             assert int(v[-1]) == 0
+
+
+def test_tuning_get_set_without_gpu(built):
+    """The launch-shape tunables are host state: get/set work without a GPU,
+    out-of-range shapes are refused, the autotuner needs a device."""
+    import maxwell_gb300 as mx
+    t0 = mx.get_tuning()
+    assert t0 == {"gram_waves": 4, "combine_ctas": 2, "residual_sites": 32}
+    mx.set_tuning(8, 1, 64)
+    assert mx.get_tuning() == {"gram_waves": 8, "combine_ctas": 1, "residual_sites": 64}
+    for bad in ((0, 2, 32), (4, 17, 32), (4, 2, 0), (65, 2, 32)):
+        with pytest.raises(RuntimeError):
+            mx.set_tuning(*bad)
+    assert mx.get_tuning() == {"gram_waves": 8, "combine_ctas": 1, "residual_sites": 64}
+    mx.set_tuning(**t0)
+    with pytest.raises(RuntimeError):
+        mx.autotune(64, 2, 4)
