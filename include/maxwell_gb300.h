@@ -396,21 +396,25 @@ typedef struct {
 int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows);
 
 /* ---------- launch-shape autotuner (no counterpart in the reference) ---------- */
-/* Launch shapes of the block kernels, process-wide: the Gram's CTAs per
- * k-point (gram_waves x SMs / K), the tiled combination's CTAs
- * (combine_ctas x SMs) and the block residual's sites per thread. */
+/* Launch shapes, process-wide: the Gram's CTAs per k-point (gram_waves x
+ * SMs / K), the tiled combination's CTAs (combine_ctas x SMs), the block
+ * residual's sites per thread, and the tiled node Gauss-Seidel sweep's strip
+ * width (positions) and band height (pairs of rows) per CTA. */
 typedef struct {
   int gram_waves;        /* 1 .. 64 */
   int combine_ctas;      /* 1 .. 16 */
   int residual_sites;    /* 1 .. 1024 */
+  int node_strip;        /* 64 or 128 */
+  int node_band;         /* 1 .. 256 */
 } mxg_tuning;
 int mxg_get_tuning(mxg_tuning *t);
 int mxg_set_tuning(const mxg_tuning *t);
 /* Times each shape's candidates (`reps` calls after one untimed call, CUDA
  * events) on synthetic blocks of n x n cells, K k-points and block m <= 16,
  * one tunable after the other, keeps the fastest and returns the choice.
- * The shapes change launch geometry only: results are the same up to the
- * order of floating-point sums. */
+ * The block kernels' shapes change launch geometry only (results the same
+ * up to the order of floating-point sums); the node sweep's strip width
+ * also moves where its truncated prefix sums start, at the 8^-9 level. */
 int mxg_autotune(int n, int K, int m, int reps, mxg_tuning *chosen);
 
 int mxg_device_ok(void);

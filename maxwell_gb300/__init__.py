@@ -209,7 +209,11 @@ def kernel_bench(n: int, K: int, m: int, reps: int = 5) -> list[dict]:
 
 class Tuning(C.Structure):
     """mxg_tuning: launch shapes of the block kernels."""
-    _fields_ = [("gram_waves", C.c_int), ("combine_ctas", C.c_int), ("residual_sites", C.c_int)]
+    _fields_ = [("gram_waves", C.c_int), ("combine_ctas", C.c_int), ("residual_sites", C.c_int),
+                ("node_strip", C.c_int), ("node_band", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 def autotune(n: int, K: int, m: int, reps: int = 3) -> dict:
@@ -219,17 +223,19 @@ def autotune(n: int, K: int, m: int, reps: int = 3) -> dict:
     r = lib().mxg_autotune(n, K, m, reps, C.byref(t))
     if r != 0:
         raise RuntimeError(f"mxg_autotune failed: {r}")
-    return {"gram_waves": t.gram_waves, "combine_ctas": t.combine_ctas, "residual_sites": t.residual_sites}
+    return t.as_dict()
 
 
 def get_tuning() -> dict:
     t = Tuning()
     check(lib().mxg_get_tuning(C.byref(t)), "mxg_get_tuning")
-    return {"gram_waves": t.gram_waves, "combine_ctas": t.combine_ctas, "residual_sites": t.residual_sites}
+    return t.as_dict()
 
 
-def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int) -> None:
-    check(lib().mxg_set_tuning(C.byref(Tuning(gram_waves, combine_ctas, residual_sites))), "mxg_set_tuning")
+def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int, node_strip: int = 128,
+               node_band: int = 16) -> None:
+    t = Tuning(gram_waves, combine_ctas, residual_sites, node_strip, node_band)
+    check(lib().mxg_set_tuning(C.byref(t)), "mxg_set_tuning")
 
 
 def header_functions() -> list[str]:

@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libmaxwell_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "bin", "nvcc")) else "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["mx_stencil.cu", "mx_dense.cu", "mx_block.cu", "mx_vec.cu"]
+CU = ["mx_stencil.cu", "mx_dense.cu", "mx_block.cu", "mx_vec.cu", "mx_nodegs.cu"]
 C = ["mx_abi.c", "mx_solver.c", "mx_kbench.c"]
 
 

@@ -576,7 +576,20 @@ static int gs_n(double a, const node2d_gpu *b, node2d_gpu *x, int dir)
 {
   const grid2d_gpu *g = x->gr;
   int e;
+  void *y = 0;
   if(b->prec != x->prec || b->m != x->m) return MXG_EINVAL;
+  if(mxk_node_gs_oop_ok(g->n, x->m, x->prec) && cudaMalloc(&y, nlen(x) * mxk_elem_size(x->prec)) == cudaSuccess) {
+    /* the tiled sweep into a scratch vector: x -> y (-> x backward for the
+     * symmetric sweep), copied back after a single one */
+    e = mxk_node_gs_oop(g->n, x->m, g->K, g->ph, a, dir == 1, x->prec, b->d, x->d, y, g->st);
+    if(!e && dir == 2) e = mxk_node_gs_oop(g->n, x->m, g->K, g->ph, a, 1, x->prec, b->d, y, x->d, g->st);
+    else if(!e)
+      e = (int) cudaMemcpyAsync(x->d, y, nlen(x) * mxk_elem_size(x->prec), cudaMemcpyDeviceToDevice, g->st);
+    if(!e) e = (int) cudaStreamSynchronize(g->st);
+    cudaFree(y);
+    return e;
+  }
+  cudaGetLastError();
   e = mxk_node_gs(g->n, x->m, g->K, g->ph, a, dir, x->prec, b->d, x->d, g->st);
   if(!e) e = (int) cudaStreamSynchronize(g->st);
   return e;

@@ -81,6 +81,14 @@ int mxk_node_apply(int n, int m, int K, const double *phases, double alpha, doub
                    int prec, const void *x, const void *yin, void *y, mx_stream s);
 int mxk_node_gs(int n, int m, int K, const double *phases, double alpha, int dir,
                 int prec, const void *b, void *x, mx_stream s);
+/* one node GS sweep (dir 0 forward, 1 backward) read from x, written to y
+ * (tiled, three launches); for c64 blocks with m % 4 == 0 and n >= 128 */
+int mxk_node_gs_oop_ok(int n, int m, int prec);
+int mxk_node_gs_oop(int n, int m, int K, const double *phases, double alpha, int dir,
+                    int prec, const void *b, const void *x, void *y, mx_stream s);
+/* strip width (64 or 128 positions) and band height (pairs of rows) */
+int mxk_node_gs_oop_shape(int strip, int band);
+void mxk_node_gs_oop_get_shape(int *strip, int *band);
 int mxk_node_prolong(int nc, int m, int K, const double *phases, double alpha,
                      int prec, const void *c, void *f, mx_stream s);
 int mxk_node_restrict(int nc, int m, int K, const double *phases, double alpha,

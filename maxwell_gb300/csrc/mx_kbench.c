@@ -65,16 +65,25 @@ int mxg_get_tuning(mxg_tuning *t)
   t->gram_waves = q.gram_waves;
   t->combine_ctas = q.combine_ctas;
   t->residual_sites = q.residual_sites;
+  mxk_node_gs_oop_get_shape(&t->node_strip, &t->node_band);
   return 0;
 }
 
 int mxg_set_tuning(const mxg_tuning *t)
 {
-  mxk_tuning q;
+  mxk_tuning q, old;
+  int s0, b0;
   q.gram_waves = t->gram_waves;
   q.combine_ctas = t->combine_ctas;
   q.residual_sites = t->residual_sites;
-  return mxk_set_tuning(&q) ? MXG_EINVAL : 0;
+  mxk_get_tuning(&old);
+  mxk_node_gs_oop_get_shape(&s0, &b0);
+  if(mxk_set_tuning(&q)) return MXG_EINVAL;
+  if(mxk_node_gs_oop_shape(t->node_strip, t->node_band)) {
+    mxk_set_tuning(&old);
+    return MXG_EINVAL;
+  }
+  return 0;
 }
 
 int mxg_autotune(int n, int K, int m, int reps, mxg_tuning *chosen)
@@ -235,6 +244,28 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
     tune->gram_waves = base.gram_waves;
     tune->combine_ctas = base.combine_ctas;
     tune->residual_sites = base.residual_sites;
+    mxk_node_gs_oop_get_shape(&tune->node_strip, &tune->node_band);
+    if(mxk_node_gs_oop_ok(n, m, MX_C64)) {
+      /* the node sweep: strip x band */
+      static const int strips[] = {64, 128}, bands[] = {4, 8, 16, 32, 64};
+      int si, bi, bs = tune->node_strip, bb = tune->node_band;
+      best = 1e30f;
+      for(si = 0; si < 2; si++)
+        for(bi = 0; bi < 5; bi++) {
+          TRY(mxk_node_gs_oop_shape(strips[si], bands[bi]));
+          if(!mxk_node_gs_oop_ok(n, m, MX_C64)) continue;
+          TRY(mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+          TRY((int) cudaEventRecord(e0, st));
+          for(it = 0; it < reps; it++) TRY(mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+          TRY((int) cudaEventRecord(e1, st));
+          TRY((int) cudaEventSynchronize(e1));
+          TRY((int) cudaEventElapsedTime(&ms, e0, e1));
+          if(ms < best) { best = ms; bs = strips[si]; bb = bands[bi]; }
+        }
+      TRY(mxk_node_gs_oop_shape(bs, bb));
+      tune->node_strip = bs;
+      tune->node_band = bb;
+    }
     goto done;
   }
   {
@@ -258,6 +289,9 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
          mxk_node_apply(n, m, K, ph, -1.0, 1.0, MX_C64, nx, nb, nd, st));
     TIME("node_gs_forward_c64", 3 * V8 * s8, 4,
          mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st));
+    if(mxk_node_gs_oop_ok(n, m, MX_C64))
+      TIME("node_gs_tiled_c64", 3 * V8 * s8, 3,
+           mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
     TIME("node_restrict_c64", (V8 + 2 * V8 / 4) * s8, 1,
          mxk_node_restrict(n / 2, m, K, ph, 1.0, MX_C64, nd, nbc, st));
     TIME("node_prolong_c64", (V8 / 4 + 2 * V8) * s8, 1,

@@ -400,6 +400,25 @@ static int node_gs(mxg_solver *s, int l, int dir)
   return e;
 }
 
+/* nu sweeps of one direction on level l: pairs of out-of-place sweeps
+ * xg -> dg -> xg (dg is free while a level smooths), the rest in place */
+static int node_smooth(mxg_solver *s, int l, int dir, int nu)
+{
+  int i = 0;
+  if(mxk_node_gs_oop_ok(s->n[l], s->m, s->pg))
+    for(; i + 2 <= nu; i += 2) {
+      int on = prof_begin(s, l, MXG_KT_NODE_GS, (double) nlen(s, l) * 6.0 * mxk_elem_size(s->pg));
+      int e = mxk_node_gs_oop(s->n[l], s->m, s->K, s->ph, 1.0, dir, s->pg, s->bg[l], s->xg[l], s->dg[l], s->st);
+      if(!e) e = mxk_node_gs_oop(s->n[l], s->m, s->K, s->ph, 1.0, dir, s->pg, s->bg[l], s->dg[l], s->xg[l], s->st);
+      s->launches += 6;
+      prof_end(s, on);
+      if(e) return e;
+    }
+  for(; i < nu; i++)
+    TRY(node_gs(s, l, dir));
+  return 0;
+}
+
 /* vcycle_edge2d (edge2d.c:5707-5754) on b[top], x[top] with the coarse inverse */
 static int vcycle_e(mxg_solver *s, int top)
 {
@@ -429,8 +448,7 @@ static int vcycle_n(mxg_solver *s, int top)
   int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
   for(l = top; l > 0; l--) {
     int n = s->n[l];
-    for(i = 0; i < nu; i++)
-      TRY(node_gs(s, l, 0));
+    TRY(node_smooth(s, l, 0, nu));
     L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->bg[l], s->dg[l], s->st));
     L_(mxk_zero(pg, s->bg[l - 1], nlen(s, l - 1), s->st));
     L_(mxk_node_restrict(n / 2, m, K, s->ph, 1.0, pg, s->dg[l], s->bg[l - 1], s->st));
@@ -440,8 +458,7 @@ static int vcycle_n(mxg_solver *s, int top)
   for(l = 1; l <= top; l++) {
     int n = s->n[l];
     L_(mxk_node_prolong(n / 2, m, K, s->ph, 1.0, pg, s->xg[l - 1], s->xg[l], s->st));
-    for(i = 0; i < nu; i++)
-      TRY(node_gs(s, l, 1));
+    TRY(node_smooth(s, l, 1, nu));
   }
   return 0;
 }
@@ -515,8 +532,7 @@ static int hcycle_e(mxg_solver *s, int top)
     L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
     L_(mxk_adjgradient(n, m, K, s->ph, 1.0, 0, 0.0, pg, s->d[l], pg, s->bg[l], s->st));
     L_(mxk_zero(pg, s->xg[l], nlen(s, l), s->st));
-    for(i = 0; i < nu; i++)
-      TRY(node_gs(s, l, 0));
+    TRY(node_smooth(s, l, 0, nu));
     L_(mxk_gradient(n, m, K, s->ph, 1.0, pg, s->xg[l], pg, s->x[l], s->st));
     L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
     L_(mxk_zero(pg, s->b[l - 1], elen(s, l - 1), s->st));
@@ -530,8 +546,7 @@ static int hcycle_e(mxg_solver *s, int top)
     L_(mxk_edge_apply(n, m, K, s->ph, kap(s, l), -1.0, -1.0, 0, 1.0, pg, s->x[l], pg, s->b[l], s->d[l], s->st));
     L_(mxk_adjgradient(n, m, K, s->ph, 1.0, 0, 0.0, pg, s->d[l], pg, s->bg[l], s->st));
     L_(mxk_zero(pg, s->xg[l], nlen(s, l), s->st));
-    for(i = 0; i < nu; i++)
-      TRY(node_gs(s, l, 1));
+    TRY(node_smooth(s, l, 1, nu));
     L_(mxk_gradient(n, m, K, s->ph, 1.0, pg, s->xg[l], pg, s->x[l], s->st));
     for(i = 0; i < nu; i++)
       L_(mxk_edge_gs_point(n, m, K, s->ph, kap(s, l), 1.0, 1.0, 1, pg, s->b[l], s->x[l], s->st));

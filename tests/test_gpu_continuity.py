@@ -4,8 +4,9 @@ reference's code applied to the same eigenvectors: the k-points of the
 reference driver's own curve (Kivshar disc, 16^2, 14 points with corners at
 points 0, 4, 8 and 13), solved by the GPU in one wave; the raw eigenvectors
 go to the oracle, the GPU adjusts its own.  Swap counts and the reordered
-eigenvalues agree exactly, the Chern partial sums and the adjusted
-eigenvectors to 1e-9."""
+eigenvalues agree exactly, the Chern partial sums and the adjusted wanted
+eigenvectors to 1e-9, the block's remaining vectors to 1e-9 up to a unit
+factor each."""
 import numpy as np
 import pytest
 
@@ -41,6 +42,17 @@ def test_continuity_matches_oracle(oracle, golden, continuity):
     assert np.array_equal(sign_g, sign_o)
     assert np.array_equal(lam_g, lam_o)
     assert np.abs(chern_g - chern_o).max() < 1e-9
-    assert np.abs(adj - v_o).max() < 1e-9 * np.abs(v_o).max()
+    # the wanted vectors exactly; the block's other vectors are not converged,
+    # and where one of them changes band between neighbouring points its
+    # overlap with the previous point's vector (whose phase the adjustment
+    # takes) is rounding noise on both sides, as is every phase after it in
+    # the chain: those agree up to one unit factor per vector
+    scale = np.abs(v_o).max()
+    assert np.abs(adj[:, :ie] - v_o[:, :ie]).max() < 1e-9 * scale
+    for l in range(nk):
+        for i in range(ie, m):
+            z = np.vdot(v_o[l, i], adj[l, i])
+            ph = z / abs(z)
+            assert np.abs(adj[l, i] - ph * v_o[l, i]).max() < 1e-9 * scale, (l, i)
     if continuity == "n":
         assert np.array_equal(adj, raw)

@@ -80,7 +80,8 @@ def test_afw_smoother(oracle, setup, prec, direction):
 
 
 @pytest.mark.parametrize("n, m, prec", [(16, 4, mx.C64), (80, 4, mx.C64), (256, 16, mx.C64), (128, 16, mx.C128),
-                                         (128, 16, mx.CDD), (32, 1, mx.C64), (48, 7, mx.C64), (24, 7, mx.C128)])
+                                         (128, 16, mx.CDD), (32, 1, mx.C64), (48, 7, mx.C64), (24, 7, mx.C128),
+                                         (128, 12, mx.C64), (512, 4, mx.C64)])
 @pytest.mark.parametrize("direction", [0, 1, 2])
 def test_node_gs_even_block(oracle, n, m, prec, direction):
     """Node Gauss-Seidel against the oracle: a row in one segment (n = 16,
@@ -98,6 +99,32 @@ def test_node_gs_even_block(oracle, n, m, prec, direction):
     want = np.array([[oracle.gs_node(n, *FACTORS[k], 1.0, direction, v_[k, i], w_[k, i]) for i in range(m)]
                      for k in range(K)])
     assert rel(nw.get(), want) < (2e-5 if prec == mx.C64 else 1e-11)
+
+
+@pytest.mark.parametrize("strip, band", [(64, 1), (64, 5), (128, 3), (128, 64)])
+@pytest.mark.parametrize("direction", [0, 1, 2])
+def test_node_gs_tiled_shapes(oracle, strip, band, direction):
+    """The tiled out-of-place node sweep (c64 blocks, m a multiple of 4,
+    n >= 128) under several strip widths and band heights -- bands of one
+    pair, bands that do not divide the (n-2)/2 pairs, a band taller than
+    the grid -- against the oracle's in-place sweep: the strips at both
+    ends wrap through the seam, the first band reads the new row 0 and the
+    last one the old row n-1."""
+    rng = np.random.default_rng(11)
+    n, m, K = 256, 8, 3
+    default = mx.get_tuning()
+    try:
+        mx.set_tuning(**dict(default, node_strip=strip, node_band=band))
+        g = mx.Grid(n, K, None, FACTORS)
+        v_, w_ = cv(rng, K, m, n * n), cv(rng, K, m, n * n)
+        nv, nw = mx.Node(g, m, mx.C64, v_), mx.Node(g, m, mx.C64, w_)
+        fn = [mx.lib().gsforward_node2d_gpu, mx.lib().gsbackward_node2d_gpu, mx.lib().gssymm_node2d_gpu][direction]
+        mx.check(fn(mx.fz(0.7), nv.h, nw.h))
+    finally:
+        mx.set_tuning(**default)
+    want = np.array([[oracle.gs_node(n, *FACTORS[k], 0.7, direction, v_[k, i], w_[k, i]) for i in range(m)]
+                     for k in range(K)])
+    assert rel(nw.get(), want) < 2e-5
 
 
 @pytest.mark.parametrize("prec", [mx.C128, mx.CDD, mx.C64])
