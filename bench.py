@@ -475,9 +475,10 @@ def run_config5(args):
 def run_surface(args):
     """The full-zone surface (exp_blochsurf): 256^2 cells, four discs eps = 10
     of radius 0.15 centred at (0.25|0.75, 0.25|0.75), a 32 x 32 k-grid over
-    [-pi, pi]^2 solved in waves of 64 (two rows; every wave after the first
-    starts from the Rayleigh-Ritz extrapolation over the same slots of the
-    three waves before it), 12 pairs with block 16 via LOBPCG, mixed
+    [-pi, pi]^2 solved in waves of --wave k-points (64: two rows), every wave
+    after the first started as --extrapolation says (by default from the
+    Rayleigh-Ritz extrapolation over the same slots of the three waves before
+    it), 12 pairs with block 16 via LOBPCG, mixed
     precision, relative residual 1e-8.  Not the headline metric: one JSON
     line of k-points/s."""
     import maxwell_gb300 as mx
@@ -524,8 +525,9 @@ def main():
     ap.add_argument("--surface", action="store_true", help="the full-zone surface workload instead of the metric")
     ap.add_argument("--config5", action="store_true", help="the 2048^2 block-32 workload instead of the metric")
     ap.add_argument("--wave", type=int, default=64, help="k-points per wave of the --surface workload")
-    ap.add_argument("--extrapolation", default="2", choices=["n", "1", "2"],
-                    help="warm start of the --surface workload's later waves")
+    ap.add_argument("--extrapolation", default="2", choices=["n", "1", "2", "c"],
+                    help="start of the --surface workload's later waves: warm from the waves before "
+                         "('n', or Rayleigh-Ritz over 2 or 3 waves '1', '2') or cold ('c')")
     ap.add_argument("--autotune", action="store_true",
                     help="choose the block kernels' launch shapes on the workload's sizes before warm-up")
     args = ap.parse_args()

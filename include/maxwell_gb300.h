@@ -278,7 +278,8 @@ typedef struct {
   int extrapolation;     /* start of every wave after the first, from the same slots of
                           * earlier waves (exp_bloch2d.c:814-895, maxwell_extra):
                           * 'n' or 0 their eigenvectors, '1' Rayleigh-Ritz over the last
-                          * two waves, '2' over the last three */
+                          * two waves, '2' over the last three; 'c' no warm start, every
+                          * wave from the nested iteration */
   int refine;            /* 1: after the finest level converges, one more block step with
                           * every search column in the Ritz basis (the refinement sweep
                           * of the 2048^2 configuration), residuals recomputed after it */
@@ -341,7 +342,7 @@ typedef struct {
   const char *pattern;   /* "Permittivity pattern" of the header */
   int n0, L;             /* coarse grid intervals, refinement levels */
   int chern_vectors;
-  int extrapolation;     /* 'n', '1', '2' */
+  int extrapolation;     /* 'n', '1', '2', 'c' */
   int stopping;          /* 'r' residual, 'f' fixed steps */
   int continuity;        /* 'n', 's', 'r' */
 } mxg_protocol_info;
@@ -404,7 +405,7 @@ typedef struct {
   int gram_waves;        /* 1 .. 64 */
   int combine_ctas;      /* 1 .. 16 */
   int residual_sites;    /* 1 .. 1024 */
-  int node_strip;        /* 64 or 128 */
+  int node_strip;        /* 0 (the in-place row kernels), 64 or 128 */
   int node_band;         /* 1 .. 256 */
 } mxg_tuning;
 int mxg_get_tuning(mxg_tuning *t);

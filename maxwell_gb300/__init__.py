@@ -232,7 +232,7 @@ def get_tuning() -> dict:
     return t.as_dict()
 
 
-def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int, node_strip: int = 128,
+def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int, node_strip: int = 0,
                node_band: int = 16) -> None:
     t = Tuning(gram_waves, combine_ctas, residual_sites, node_strip, node_band)
     check(lib().mxg_set_tuning(C.byref(t)), "mxg_set_tuning")

@@ -245,22 +245,32 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
     tune->combine_ctas = base.combine_ctas;
     tune->residual_sites = base.residual_sites;
     mxk_node_gs_oop_get_shape(&tune->node_strip, &tune->node_band);
-    if(mxk_node_gs_oop_ok(n, m, MX_C64)) {
-      /* the node sweep: strip x band */
-      static const int strips[] = {64, 128}, bands[] = {4, 8, 16, 32, 64};
-      int si, bi, bs = tune->node_strip, bb = tune->node_band;
+    {
+      /* the node sweep: the in-place row kernels (strip 0) against the
+       * tiled out-of-place sweep with each strip x band (two sweeps, so
+       * that both leave the result where the in-place pair does) */
+      static const int strips[] = {0, 64, 128}, bands[] = {4, 8, 16, 32, 64};
+      int si, bi, bs = 0, bb = tune->node_band;
       best = 1e30f;
-      for(si = 0; si < 2; si++)
-        for(bi = 0; bi < 5; bi++) {
-          TRY(mxk_node_gs_oop_shape(strips[si], bands[bi]));
-          if(!mxk_node_gs_oop_ok(n, m, MX_C64)) continue;
-          TRY(mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+      for(si = 0; si < 3; si++)
+        for(bi = 0; bi < (si ? 5 : 1); bi++) {
+          int ok;
+          TRY(mxk_node_gs_oop_shape(strips[si], si ? bands[bi] : bb));
+          ok = mxk_node_gs_oop_ok(n, m, MX_C64);
+          if(si && !ok) continue;
+#define SWEEP2()                                                                             \
+          (ok ? (mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st)                \
+                 || mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nd, nx, st))            \
+              : (mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st)                        \
+                 || mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st)))
+          TRY(SWEEP2());
           TRY((int) cudaEventRecord(e0, st));
-          for(it = 0; it < reps; it++) TRY(mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+          for(it = 0; it < reps; it++) TRY(SWEEP2());
+#undef SWEEP2
           TRY((int) cudaEventRecord(e1, st));
           TRY((int) cudaEventSynchronize(e1));
           TRY((int) cudaEventElapsedTime(&ms, e0, e1));
-          if(ms < best) { best = ms; bs = strips[si]; bb = bands[bi]; }
+          if(ms < best) { best = ms; bs = strips[si]; if(si) bb = bands[bi]; }
         }
       TRY(mxk_node_gs_oop_shape(bs, bb));
       tune->node_strip = bs;
@@ -289,9 +299,16 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
          mxk_node_apply(n, m, K, ph, -1.0, 1.0, MX_C64, nx, nb, nd, st));
     TIME("node_gs_forward_c64", 3 * V8 * s8, 4,
          mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st));
-    if(mxk_node_gs_oop_ok(n, m, MX_C64))
-      TIME("node_gs_tiled_c64", 3 * V8 * s8, 3,
-           mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+    {
+      /* the tiled sweep at its default shape, whatever the current one */
+      int s0, b0;
+      mxk_node_gs_oop_get_shape(&s0, &b0);
+      mxk_node_gs_oop_shape(128, 16);
+      if(mxk_node_gs_oop_ok(n, m, MX_C64))
+        TIME("node_gs_tiled_c64", 3 * V8 * s8, 3,
+             mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+      mxk_node_gs_oop_shape(s0, b0);
+    }
     TIME("node_restrict_c64", (V8 + 2 * V8 / 4) * s8, 1,
          mxk_node_restrict(n / 2, m, K, ph, 1.0, MX_C64, nd, nbc, st));
     TIME("node_prolong_c64", (V8 / 4 + 2 * V8) * s8, 1,

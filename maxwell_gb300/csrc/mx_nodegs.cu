@@ -310,14 +310,15 @@ int run_sweep(int n, int m, int K, const double* ph, double alpha, int bwd, int 
   return 0;
 }
 
-int g_strip = 128, g_band = 16;
+// strip 0: the tiled sweep is off and callers use the in-place row kernels
+int g_strip = 0, g_band = 16;
 
 }  // namespace
 
 // The strip width for n: the largest of 128 and 64 that divides n and
 // leaves the staged window (T + 2D + 6 positions) shorter than a row.
 static int strip_for(int n) {
-  for (int T = g_strip; T >= 64; T /= 2)
+  for (int T = g_strip; T >= 64; T /= 2)   // (no strip when g_strip is 0)
     if (n % T == 0 && T + 2 * 8 + 6 < n) return T;
   return 0;
 }
@@ -327,7 +328,7 @@ extern "C" int mxk_node_gs_oop_ok(int n, int m, int prec) {
 }
 
 extern "C" int mxk_node_gs_oop_shape(int strip, int band) {
-  if ((strip != 64 && strip != 128) || band < 1 || band > 256) return (int) cudaErrorInvalidValue;
+  if ((strip != 0 && strip != 64 && strip != 128) || band < 1 || band > 256) return (int) cudaErrorInvalidValue;
   g_strip = strip;
   g_band = band;
   return 0;

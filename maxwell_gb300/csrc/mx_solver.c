@@ -181,7 +181,8 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   double *kk[MAXL];
   if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 32
      || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 2
-     || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'))
+     || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'
+         && o->extrapolation != 'c'))
     return 0;
   s = calloc(1, sizeof(mxg_solver));
   s->o = *o;
@@ -911,7 +912,7 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
     TRY(set_bloch(s, Ka, xf + k0, yf + k0));
     TRY((int) cudaEventRecord(s->ev0, s->st));
     TRY(factor_coarse(s));
-    if(!s->have_prev || s->K_prev != K) {
+    if(!s->have_prev || s->K_prev != K || s->o.extrapolation == 'c') {
       double tc = now_s();
       TRY(cold_start(s, Ka));
       if(s->timing) fprintf(stderr, "wave %d: cold start incl. finest-level steps %.3f s\n", w, now_s() - tc);

@@ -129,7 +129,7 @@ def test_tuning_get_set_without_gpu(built):
     out-of-range shapes are refused, the autotuner needs a device."""
     import maxwell_gb300 as mx
     t0 = mx.get_tuning()
-    assert t0 == {"gram_waves": 4, "combine_ctas": 2, "residual_sites": 32, "node_strip": 128, "node_band": 16}
+    assert t0 == {"gram_waves": 4, "combine_ctas": 2, "residual_sites": 32, "node_strip": 0, "node_band": 16}
     mx.set_tuning(8, 1, 64, 64, 8)
     want = {"gram_waves": 8, "combine_ctas": 1, "residual_sites": 64, "node_strip": 64, "node_band": 8}
     assert mx.get_tuning() == want

@@ -26,7 +26,7 @@ def test_autotune_choice_and_solve(golden):
         assert t["gram_waves"] in (1, 2, 4, 8, 16)
         assert t["combine_ctas"] in (1, 2, 3, 4)
         assert t["residual_sites"] in (8, 16, 32, 64, 128)
-        assert t["node_strip"] in (64, 128) and t["node_band"] in (4, 8, 16, 32, 64)
+        assert t["node_strip"] in (0, 64, 128) and t["node_band"] in (4, 8, 16, 32, 64)
         assert mx.get_tuning() == t
         # the extreme shapes too
         for shape in ({"gram_waves": 1, "combine_ctas": 1, "residual_sites": 128, "node_strip": 64, "node_band": 1},

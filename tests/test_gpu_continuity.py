@@ -4,9 +4,9 @@ reference's code applied to the same eigenvectors: the k-points of the
 reference driver's own curve (Kivshar disc, 16^2, 14 points with corners at
 points 0, 4, 8 and 13), solved by the GPU in one wave; the raw eigenvectors
 go to the oracle, the GPU adjusts its own.  Swap counts and the reordered
-eigenvalues agree exactly, the Chern partial sums and the adjusted wanted
-eigenvectors to 1e-9, the block's remaining vectors to 1e-9 up to a unit
-factor each."""
+eigenvalues agree exactly, the Chern partial sums to 1e-9, the adjusted
+eigenvectors to 1e-9 up to a unit factor each, and the GPU's adjusted
+vectors make every overlap with their guess real and non-negative."""
 import numpy as np
 import pytest
 
@@ -42,17 +42,27 @@ def test_continuity_matches_oracle(oracle, golden, continuity):
     assert np.array_equal(sign_g, sign_o)
     assert np.array_equal(lam_g, lam_o)
     assert np.abs(chern_g - chern_o).max() < 1e-9
-    # the wanted vectors exactly; the block's other vectors are not converged,
-    # and where one of them changes band between neighbouring points its
-    # overlap with the previous point's vector (whose phase the adjustment
-    # takes) is rounding noise on both sides, as is every phase after it in
-    # the chain: those agree up to one unit factor per vector
+    # The adjusted vectors: where a vector changes band between neighbouring
+    # points (the block's unconverged vectors, and with 's' crossing wanted
+    # ones), its overlap with the previous point's vector -- whose phase the
+    # adjustment takes -- is rounding noise on both sides, and the phase
+    # difference travels down the chain (the Chern sums, made of relative
+    # phases, do not see it).  So every adjusted vector equals the oracle's
+    # up to one unit factor, and the GPU's own vectors meet the rule itself:
+    # e_i^H M guess_i real and non-negative, guess_i the previous point's
+    # vector (or 2 e_i(l-1) - e_i(l-2) away from corners)
     scale = np.abs(v_o).max()
-    assert np.abs(adj[:, :ie] - v_o[:, :ie]).max() < 1e-9 * scale
     for l in range(nk):
-        for i in range(ie, m):
+        for i in range(m):
             z = np.vdot(v_o[l, i], adj[l, i])
             ph = z / abs(z)
             assert np.abs(adj[l, i] - ph * v_o[l, i]).max() < 1e-9 * scale, (l, i)
+    if continuity != "n":
+        for l in range(1, nk):
+            for i in range(m):
+                prev2 = adj[l - 2, i] if l > 1 else np.zeros_like(adj[0, i])
+                guess = adj[l - 1, i] if vertex[l - 1] else 2 * adj[l - 1, i] - prev2
+                p = oracle.massprod_edge(n, *fac[l], guess, adj[l, i])
+                assert abs(p.imag) <= 1e-9 * abs(p) and p.real >= 0, (l, i, p)
     if continuity == "n":
         assert np.array_equal(adj, raw)
