@@ -31,7 +31,8 @@
 // so one code path serves both directions.
 //
 // Each step of a CTA stages, by cp.async one step ahead, the two next old
-// rows and the two b rows; a step is four phases separated by barriers:
+// rows (b goes to registers one phase ahead); a step is four phases
+// separated by barriers:
 // betas of the odd row (runs of RL positions per thread, a sliding window
 // over the neighbour rows), its truncated prefix sums (Horner over the D
 // betas before a run, then the recurrence), the betas of the even row, its
@@ -65,183 +66,247 @@ struct NgsArgs {
 
 // The CTA's view: strip [t0, t0+T) of k-point k, vectors [v0, v0+VB).
 // Shared buffers hold W = T + HL + HR positions x VB vectors, position u
-// at slot u - base.
-template <typename S, typename R, int D, int VB, int RL>
+// at slot u - base.  A thread has at most one run of RL positions per
+// phase (task = thread); runs away from the row ends and the seam take a
+// fast path with fixed shared-memory offsets and no per-position tests,
+// and the right-hand side of a fast run is loaded into registers one phase
+// before it is used.
+template <typename S, typename R, int D, int VB, int RL, int T, int NTH>
 struct Tile {
-  static constexpr int HL = 2 * D + 2, HR = 4;
-  static constexpr int CPS = VB * (int) sizeof(S) / 16;   // 16-byte chunks per site
-  int n, m, T, W, bwd, t0, base, v0, k;
+  static constexpr int HL = 2 * D + 2, HR = 4, W = T + HL + HR;
+  static constexpr int EPC = 16 / (int) sizeof(S);        // elements per 16-byte chunk
+  static constexpr int NCH = W * VB / EPC;                 // chunks per staged row
+  static constexpr int NR = (NCH + NTH - 1) / NTH;         // chunks per thread
+  int n, m, bwd, t0, base, v0, k;
   cx<R> pl, pr, pb, pa;   // phases of positions u < 0, u >= n, rows s < 0, s >= n
   R inv_ac, third;
+  int goff[NR], soff[NR];  // this thread's chunks: element offsets in a row / in a buffer
 
-  __device__ Tile(const NgsArgs& a, int strip, int g, int k_) {
-    n = a.n; m = a.m; T = a.T; W = T + HL + HR; bwd = a.bwd;
+  __device__ Tile(const NgsArgs& a, int strip, int g, int k_, int tid) {
+    n = a.n; m = a.m; bwd = a.bwd;
     t0 = strip * T; base = t0 - HL; v0 = g * VB; k = k_;
     const Seam<R> sm = seam_load<R>(a.ph, a.K, k, n);
     const cx<R> xs = bwd ? conjc(sm.xf) : sm.xf, ys = bwd ? conjc(sm.yf) : sm.yf;
     pl = conjc(xs); pr = xs; pb = conjc(ys); pa = ys;
     inv_ac = sget<R>(a.inv_ac); third = sget<R>(a.third);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const int q = tid + r * NTH;
+      const int w = q * EPC / VB, e = q * EPC - w * VB;
+      const int c = canon(base + w);
+      goff[r] = (bwd ? n - 1 - c : c) * m + e;
+      soff[r] = q < NCH ? w * VB + e : -1;
+    }
   }
   __device__ __forceinline__ int canon(int u) const { return u < 0 ? u + n : (u >= n ? u - n : u); }
-  // element (sweep row s in [-1, n], canonical position c) of a node array
-  __device__ __forceinline__ size_t at(int s, int c) const {
-    const int sj = s < 0 ? s + n : (s >= n ? s - n : s);
-    const int j = bwd ? n - 1 - sj : sj, i = bwd ? n - 1 - c : c;
-    return (((size_t) k * n + j) * n + i) * m + v0;
-  }
-  // stage the window of sweep row s of src into buf (raw values)
-  __device__ __forceinline__ void stage(S* buf, const S* src, int s, int tid, int nth) const {
-    const int nch = W * CPS;
-    for (int q = tid; q < nch; q += nth) {
-      const int w = q / CPS, part = q - w * CPS;
-      const char* g = reinterpret_cast<const char*>(src + at(s, canon(base + w))) + 16 * part;
-      cpa16(reinterpret_cast<char*>(buf + (size_t) w * VB) + 16 * part, g);
-    }
-  }
-  // multiply the wrapped positions of a staged row (and the whole row, if
-  // row s lies across the seam) by their phases
-  __device__ __forceinline__ void fix(S* buf, int s, int tid, int nth) const {
-    const bool rw = s < 0 || s >= n;
-    const cx<R> rp = s < 0 ? pb : pa;
-    for (int q = tid; q < W * VB; q += nth) {
-      const int u = base + q / VB;
-      if (!rw && u >= 0 && u < n) continue;
-      cx<R> p = u < 0 ? pl : (u >= n ? pr : mkc(rc<R>(1.0f), Real<R>::zero()));
-      if (rw) p = p * rp;
-      S* e = buf + q;
-      Store<S, R>::st(e, p * Store<S, R>::ld(e));
-    }
-  }
-  // the row s of a node array at position 0 of vector v0
+  __device__ __forceinline__ int col(int u) const { return bwd ? n - 1 - u : u; }   // u in [0, n)
+  // the row s (sweep order, -1 and n through the seam) of a node array at i = 0
   __device__ __forceinline__ size_t row(int s) const {
-    const int j = bwd ? n - 1 - s : s;
+    const int sj = s < 0 ? s + n : (s >= n ? s - n : s);
+    const int j = bwd ? n - 1 - sj : sj;
     return (((size_t) k * n + j) * n) * m + v0;
   }
-  __device__ __forceinline__ bool edge() const { return base < 0 || t0 + T + HR > n; }
+  __device__ __forceinline__ void stage(S* buf, const S* src, int s) const {
+    const S* rp = src + row(s);
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+      if (soff[r] >= 0) cpa16(buf + soff[r], rp + goff[r]);
+  }
+  // multiply the wrapped positions of a staged row (the whole row, if row s
+  // lies across the seam) by their phases
+  __device__ void fix(S* buf, int s, int tid) const {
+    const bool rw = s < 0 || s >= n;
+    const cx<R> one = mkc(rc<R>(1.0f), Real<R>::zero());
+    const cx<R> rp = rw ? (s < 0 ? pb : pa) : one;
+    const int lo = rw ? W : (base < 0 ? -base : 0);            // slots [0, lo) wrap left
+    const int hi = rw ? W : (base + W > n ? n - base : W);     // slots [hi, W) wrap right
+    for (int q = tid; q < W * VB; q += NTH) {
+      const int w = q / VB, u = base + w;
+      if (!rw && w >= lo && w < hi) continue;
+      const cx<R> p = (u < 0 ? pl : (u >= n ? pr : one)) * rp;
+      Store<S, R>::st(buf + q, p * Store<S, R>::ld(buf + q));
+    }
+  }
+  __device__ __forceinline__ bool edge() const { return base < 0 || base + W > n; }
   __device__ __forceinline__ cx<R> L(const S* buf, int u, int v) const {
     return Store<S, R>::ld(buf + (size_t) (u - base) * VB + v);
   }
+  // b of the row s at position u, through the seam
+  __device__ __forceinline__ cx<R> ldb(const S* B, int s, int u, int v) const {
+    const int c = canon(u);
+    cx<R> z = Store<S, R>::ld(B + row(s) + (size_t) col(c) * m + v);
+    if (u < 0) z = pl * z;
+    else if (u >= n) z = pr * z;
+    return z;
+  }
+  // the run [p0, p0+len) of task `task` over [ua, ub); fast: a full run
+  // whose betas read canonical positions 1..n-2 only
+  __device__ __forceinline__ bool run_of(int task, int ua, int ub, int& v, int& p0, int& len) const {
+    v = task % VB;
+    p0 = ua + (task / VB) * RL;
+    len = ub - p0 < RL ? ub - p0 : RL;
+    return len == RL && p0 - 1 >= 1 && p0 + RL + 1 <= n - 2;
+  }
+  // right-hand side of a fast beta run, into registers
+  __device__ __forceinline__ void loadb(int task, int ua, int ub, const S* B, int s, cx<R> (&bv)[RL]) const {
+    int v, p0, len;
+    if (task >= ((ub - ua + RL - 1) / RL) * VB || !run_of(task, ua, ub, v, p0, len)) return;
+    const S* bp = B + row(s) + (size_t) col(p0) * m + v;
+    const int st = bwd ? -m : m;
+#pragma unroll
+    for (int q = 0; q < RL; q++) bv[q] = Store<S, R>::ld(bp + q * st);
+  }
 
-  // betas of positions [ua, ub) of a row: below / above are the rows s-1 and
-  // s+1 (old or new), own the row's old values, bb its right-hand side
-  __device__ void betas(int ua, int ub, const S* below, const S* above, const S* own, const S* bb, S* beta,
-                        int tid, int nth) const {
+  // betas of positions [ua, ub) of the row s: below / above are the rows
+  // s-1 and s+1 (old or new), own the row's old values; b in bv for a fast
+  // run, else read here
+  __device__ void betas(int task, int ua, int ub, const S* below, const S* above, const S* own, const S* B,
+                        int s, const cx<R> (&bv)[RL], S* beta) const {
+    int v, p0, len;
+    if (task >= ((ub - ua + RL - 1) / RL) * VB) return;
     const R eighth = rc<R>(0.125f);
-    const int nrun = (ub - ua + RL - 1) / RL;
-    for (int task = tid; task < nrun * VB; task += nth) {
-      const int v = task % VB, p0 = ua + (task / VB) * RL, p1 = p0 + RL < ub ? p0 + RL : ub;
-      cx<R> cm = L(below, p0 - 1, v) + L(above, p0 - 1, v);
-      cx<R> c0 = L(below, p0, v) + L(above, p0, v);
-      for (int u = p0; u < p1; u++) {
-        const cx<R> cp = L(below, u + 1, v) + L(above, u + 1, v);
-        const int c = canon(u);
-        cx<R> nxt;
-        if (c == n - 1) {
-          // the new value at the cut u+1, from old values around it
-          const cx<R> cpp = L(below, u + 2, v) + L(above, u + 2, v);
-          nxt = scal(inv_ac, L(bb, u + 1, v) + scal(third, L(own, u + 2, v) + ((c0 + cp) + cpp)))
-                + scal(eighth, L(own, u, v));
-        } else {
-          nxt = L(own, u + 1, v);
-        }
-        cx<R> be = scal(inv_ac, L(bb, u, v) + scal(third, nxt + ((cm + c0) + cp)));
-        if (c == 0) be = be + scal(eighth, L(own, u - 1, v));
-        Store<S, R>::st(beta + (size_t) (u - base) * VB + v, be);
+    if (run_of(task, ua, ub, v, p0, len)) {
+      const int o = (p0 - base) * VB + v;
+      const S *pb_ = below + o, *pa_ = above + o, *po = own + o;
+      S* pz = beta + o;
+      cx<R> cm = Store<S, R>::ld(pb_ - VB) + Store<S, R>::ld(pa_ - VB);
+      cx<R> c0 = Store<S, R>::ld(pb_) + Store<S, R>::ld(pa_);
+#pragma unroll
+      for (int q = 0; q < RL; q++) {
+        const cx<R> cp = Store<S, R>::ld(pb_ + (q + 1) * VB) + Store<S, R>::ld(pa_ + (q + 1) * VB);
+        const cx<R> nb = (cm + c0) + cp;
+        Store<S, R>::st(pz + q * VB, scal(inv_ac, bv[q] + scal(third, Store<S, R>::ld(po + (q + 1) * VB) + nb)));
         cm = c0;
         c0 = cp;
       }
+      return;
+    }
+    cx<R> cm = L(below, p0 - 1, v) + L(above, p0 - 1, v);
+    cx<R> c0 = L(below, p0, v) + L(above, p0, v);
+    for (int u = p0; u < p0 + len; u++) {
+      const cx<R> cp = L(below, u + 1, v) + L(above, u + 1, v);
+      const int c = canon(u);
+      cx<R> nxt;
+      if (c == n - 1) {
+        // the new value at the cut u+1, from old values around it
+        const cx<R> cpp = L(below, u + 2, v) + L(above, u + 2, v);
+        nxt = scal(inv_ac, ldb(B, s, u + 1, v) + scal(third, L(own, u + 2, v) + ((c0 + cp) + cpp)))
+              + scal(eighth, L(own, u, v));
+      } else {
+        nxt = L(own, u + 1, v);
+      }
+      cx<R> be = scal(inv_ac, ldb(B, s, u, v) + scal(third, nxt + ((cm + c0) + cp)));
+      if (c == 0) be = be + scal(eighth, L(own, u - 1, v));
+      Store<S, R>::st(beta + (size_t) (u - base) * VB + v, be);
+      cm = c0;
+      c0 = cp;
     }
   }
   // new values of positions [ua, ub): into out (shared, may be null) and,
   // for positions in [t0, t0+T), into the row of y at yrow (may be null)
-  __device__ void prefix(int ua, int ub, const S* beta, S* out, S* yrow, int tid, int nth) const {
+  __device__ void prefix(int task, int ua, int ub, const S* beta, S* out, S* yrow) const {
+    int v, p0, len;
+    if (task >= ((ub - ua + RL - 1) / RL) * VB) return;
+    run_of(task, ua, ub, v, p0, len);
     const R eighth = rc<R>(0.125f);
-    const int nrun = (ub - ua + RL - 1) / RL;
-    for (int task = tid; task < nrun * VB; task += nth) {
-      const int v = task % VB, p0 = ua + (task / VB) * RL, p1 = p0 + RL < ub ? p0 + RL : ub;
-      const int c0 = canon(p0), dmax = c0 < D ? c0 : D;
-      cx<R> acc = czero<R>();
-      for (int d = dmax; d >= 1; d--) acc = scal(eighth, acc) + L(beta, p0 - d, v);
-      for (int u = p0; u < p1; u++) {
-        const cx<R> be = L(beta, u, v);
-        acc = canon(u) == 0 ? be : scal(eighth, acc) + be;
-        if (out) Store<S, R>::st(out + (size_t) (u - base) * VB + v, acc);
-        if (yrow && u >= t0 && u < t0 + T) Store<S, R>::st(yrow + (size_t) (bwd ? n - 1 - u : u) * m + v, acc);
+    // a cut (position 0 mod n) among the D betas before the run or in it
+    const int a = p0 - D, b = p0 + len - 1;
+    const bool cut = (a <= 0 && b >= 0) || (a <= n && b >= n);
+    cx<R> acc = czero<R>();
+    if (len == RL && !cut) {
+      const int o = (p0 - base) * VB + v;
+      const S* pz = beta + o;
+#pragma unroll
+      for (int d = D; d >= 1; d--) acc = scal(eighth, acc) + Store<S, R>::ld(pz - d * VB);
+      const bool in0 = p0 >= t0 && p0 + RL <= t0 + T;
+      S* yp = yrow ? yrow + (size_t) (p0 >= 0 && p0 < n ? col(p0) : 0) * m + v : nullptr;
+      const int st = bwd ? -m : m;
+#pragma unroll
+      for (int q = 0; q < RL; q++) {
+        acc = scal(eighth, acc) + Store<S, R>::ld(pz + q * VB);
+        if (out) Store<S, R>::st(out + o + q * VB, acc);
+        if (yp && (in0 || (p0 + q >= t0 && p0 + q < t0 + T))) Store<S, R>::st(yp + q * st, acc);
       }
+      return;
+    }
+    const int c0 = canon(p0), dmax = c0 < D ? c0 : D;
+    for (int d = dmax; d >= 1; d--) acc = scal(eighth, acc) + L(beta, p0 - d, v);
+    for (int u = p0; u < p0 + len; u++) {
+      const cx<R> be = L(beta, u, v);
+      acc = canon(u) == 0 ? be : scal(eighth, acc) + be;
+      if (out) Store<S, R>::st(out + (size_t) (u - base) * VB + v, acc);
+      if (yrow && u >= t0 && u < t0 + T) Store<S, R>::st(yrow + (size_t) col(u) * m + v, acc);
     }
   }
 };
 
 // launch 2: rows 1..n-2, grid (G x strips, bands, K)
-template <typename S, typename R, int D, int VB, int RL>
-__global__ void __launch_bounds__(128) k_node_gs_tile(NgsArgs a) {
-  using TT = Tile<S, R, D, VB, RL>;
+template <typename S, typename R, int D, int VB, int RL, int T, int NTH>
+__global__ void __launch_bounds__(NTH, 5) k_node_gs_tile(NgsArgs a) {
+  using TT = Tile<S, R, D, VB, RL, T, NTH>;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const TT t(a, blockIdx.x / a.G, blockIdx.x % a.G, blockIdx.z);
-  const int tid = threadIdx.x, nth = blockDim.x, n = t.n, t0 = t.t0, T = t.T;
+  const int tid = threadIdx.x;
+  const TT t(a, blockIdx.x / a.G, blockIdx.x % a.G, blockIdx.z, tid);
+  const int n = t.n, t0 = t.t0;
   const int Q = (n - 2) / 2, q0 = blockIdx.y * a.qb, q1 = q0 + a.qb < Q ? q0 + a.qb : Q;
   if (q0 >= Q) return;
-  const size_t BS = (size_t) t.W * VB;
+  constexpr int BS = TT::W * VB;
   S* sm = reinterpret_cast<S*>(smraw);
   S* old = sm;                 // 5 rows, slot s % 5
-  S* bsm = sm + 5 * BS;        // 4 rows: (step & 1) * 2 + {odd, even}
-  S* odd = sm + 9 * BS;        // 2 rows: step & 1
-  S* beta = sm + 11 * BS;
+  S* odd = sm + 5 * BS;        // 2 rows: step & 1
+  S* beta = sm + 7 * BS;
   const S* X = reinterpret_cast<const S*>(a.x);
   const S* B = reinterpret_cast<const S*>(a.b);
   S* Y = reinterpret_cast<S*>(a.y);
   const bool edge = t.edge();
   const int nsteps = q1 - q0 + 1;
+  // the phases' ranges: odd betas, odd new values, even betas / new values
+  const int ob0 = t0 - 2 * D - 1, ob1 = t0 + T + 2, on0 = t0 - D - 1, on1 = t0 + T + 2;
+  const int eb0 = t0 - D, eb1 = t0 + T;
+  cx<R> bodd[RL], bev[RL];
 
   // prologue: the rows and b of the first odd row (row 0 comes from y)
   {
     const int o = 2 * q0 + 1;
-    for (int s = o - 1; s <= o + 1; s++) t.stage(old + (s % 5) * BS, s == 0 ? Y : X, s, tid, nth);
-    t.stage(bsm, B, o, tid, nth);
+    for (int s = o - 1; s <= o + 1; s++) t.stage(old + (s % 5) * BS, s == 0 ? Y : X, s);
     cpa_commit();
+    t.loadb(tid, ob0, ob1, B, o, bodd);
   }
   for (int i = 0; i < nsteps; i++) {
     const int o = 2 * (q0 + i) + 1, e = o - 1;
-    // stage step i+1: rows o+2 and o+3, b of its odd and even rows, into
-    // slots that step i-1 used last
+    // stage rows o+2 and o+3 for step i+1, into slots step i-1 used last
     if (i + 1 < nsteps) {
-      const int o2 = o + 2;
-      t.stage(old + (o2 % 5) * BS, X, o2, tid, nth);
-      if (o2 + 1 <= n - 1) t.stage(old + ((o2 + 1) % 5) * BS, X, o2 + 1, tid, nth);
-      S* bn = bsm + (size_t) ((i + 1) & 1) * 2 * BS;
-      if (o2 <= n - 2) t.stage(bn, B, o2, tid, nth);
-      t.stage(bn + BS, B, o2 - 1, tid, nth);
+      t.stage(old + ((o + 2) % 5) * BS, X, o + 2);
+      if (o + 3 <= n - 1) t.stage(old + ((o + 3) % 5) * BS, X, o + 3);
     }
     cpa_commit();
+    if (i > 0) t.loadb(tid, eb0, eb1, B, e, bev);
     cpa_wait1();
     __syncthreads();
-    S* bo = bsm + (size_t) (i & 1) * 2 * BS;
     if (edge) {
-      if (i == 0) t.fix(old + ((o - 1) % 5) * BS, o - 1, tid, nth);
-      t.fix(old + (o % 5) * BS, o, tid, nth);
-      if (o + 1 <= n - 1) t.fix(old + ((o + 1) % 5) * BS, o + 1, tid, nth);
-      if (o <= n - 2) t.fix(bo, o, tid, nth);
-      if (i > 0) t.fix(bo + BS, e, tid, nth);
+      if (i == 0) t.fix(old + ((o - 1) % 5) * BS, o - 1, tid);
+      t.fix(old + (o % 5) * BS, o, tid);
+      if (o + 1 <= n - 1) t.fix(old + ((o + 1) % 5) * BS, o + 1, tid);
       __syncthreads();
     }
     const S* above;
     if (o <= n - 2) {
-      S* on = odd + (size_t) (i & 1) * BS;
-      t.betas(t0 - 2 * D - 1, t0 + T + 2, old + ((o - 1) % 5) * BS, old + ((o + 1) % 5) * BS, old + (o % 5) * BS,
-              bo, beta, tid, nth);
+      S* on = odd + (i & 1) * BS;
+      t.betas(tid, ob0, ob1, old + ((o - 1) % 5) * BS, old + ((o + 1) % 5) * BS, old + (o % 5) * BS, B, o, bodd,
+              beta);
       __syncthreads();
       // the odd row of the next band is recomputed here, not written
-      t.prefix(t0 - D - 1, t0 + T + 2, beta, on, i < q1 - q0 ? Y + t.row(o) : nullptr, tid, nth);
+      t.prefix(tid, on0, on1, beta, on, i < q1 - q0 ? Y + t.row(o) : nullptr);
       __syncthreads();
       above = on;
     } else {
       above = old + (o % 5) * BS;   // the even row n-2 reads the old row n-1
     }
+    if (i + 1 < nsteps && o + 2 <= n - 2) t.loadb(tid, ob0, ob1, B, o + 2, bodd);
     if (i > 0) {
-      t.betas(t0 - D, t0 + T, odd + (size_t) ((i - 1) & 1) * BS, above, old + (e % 5) * BS, bo + BS, beta, tid,
-              nth);
+      t.betas(tid, eb0, eb1, odd + ((i - 1) & 1) * BS, above, old + (e % 5) * BS, B, e, bev, beta);
       __syncthreads();
-      t.prefix(t0, t0 + T, beta, nullptr, Y + t.row(e), tid, nth);
+      t.prefix(tid, eb0 + D, eb1, beta, nullptr, Y + t.row(e));
     }
     __syncthreads();
   }
@@ -251,61 +316,57 @@ __global__ void __launch_bounds__(128) k_node_gs_tile(NgsArgs a) {
 // launches 1 and 3: the single row s1 (0 or n-1 in sweep order), grid
 // (G x strips, 1, K).  Row 0 reads the old rows -1 (the seam) and 1; row
 // n-1 reads the new rows n-2 and n (the seam: row 0).
-template <typename S, typename R, int D, int VB, int RL>
-__global__ void __launch_bounds__(128) k_node_gs_single(NgsArgs a) {
-  using TT = Tile<S, R, D, VB, RL>;
+template <typename S, typename R, int D, int VB, int RL, int T, int NTH>
+__global__ void __launch_bounds__(NTH) k_node_gs_single(NgsArgs a) {
+  using TT = Tile<S, R, D, VB, RL, T, NTH>;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const TT t(a, blockIdx.x / a.G, blockIdx.x % a.G, blockIdx.z);
-  const int tid = threadIdx.x, nth = blockDim.x, t0 = t.t0, T = t.T, s = a.s1;
-  const size_t BS = (size_t) t.W * VB;
+  const int tid = threadIdx.x;
+  const TT t(a, blockIdx.x / a.G, blockIdx.x % a.G, blockIdx.z, tid);
+  const int t0 = t.t0, s = a.s1;
+  constexpr int BS = TT::W * VB;
   S* sm = reinterpret_cast<S*>(smraw);
   const S* X = reinterpret_cast<const S*>(a.x);
+  const S* B = reinterpret_cast<const S*>(a.b);
   const S* nbr = s == 0 ? X : reinterpret_cast<const S*>(a.y);
-  t.stage(sm, nbr, s - 1, tid, nth);
-  t.stage(sm + BS, nbr, s + 1, tid, nth);
-  t.stage(sm + 2 * BS, X, s, tid, nth);
-  t.stage(sm + 3 * BS, reinterpret_cast<const S*>(a.b), s, tid, nth);
+  cx<R> bv[RL];
+  t.stage(sm, nbr, s - 1);
+  t.stage(sm + BS, nbr, s + 1);
+  t.stage(sm + 2 * BS, X, s);
   cpa_commit();
+  t.loadb(tid, t0 - D, t0 + T, B, s, bv);
   cpa_wait0();
   __syncthreads();
-  t.fix(sm, s - 1, tid, nth);
-  t.fix(sm + BS, s + 1, tid, nth);
-  if (t.edge()) {
-    t.fix(sm + 2 * BS, s, tid, nth);
-    t.fix(sm + 3 * BS, s, tid, nth);
-  }
+  t.fix(sm, s - 1, tid);
+  t.fix(sm + BS, s + 1, tid);
+  if (t.edge()) t.fix(sm + 2 * BS, s, tid);
   __syncthreads();
-  t.betas(t0 - D, t0 + T, sm, sm + BS, sm + 2 * BS, sm + 3 * BS, sm + 4 * BS, tid, nth);
+  t.betas(tid, t0 - D, t0 + T, sm, sm + BS, sm + 2 * BS, B, s, bv, sm + 3 * BS);
   __syncthreads();
-  t.prefix(t0, t0 + T, sm + 4 * BS, nullptr, reinterpret_cast<S*>(a.y) + t.row(s), tid, nth);
+  t.prefix(tid, t0, t0 + T, sm + 3 * BS, nullptr, reinterpret_cast<S*>(a.y) + t.row(s));
 }
 
-template <typename S, typename R, int D, int VB, int RL>
-int run_sweep(int n, int m, int K, const double* ph, double alpha, int bwd, int T, int qb, const void* b,
-              const void* x, void* y, cudaStream_t st) {
-  using TT = Tile<S, R, D, VB, RL>;
+template <typename S, typename R, int D, int VB, int RL, int T>
+int run_sweep(int n, int m, int K, const double* ph, double alpha, int bwd, int qb, const void* b, const void* x,
+              void* y, cudaStream_t st) {
+  // one run per thread in every phase: the longest phase has T + 2D + 3 positions
+  constexpr int NTH = (VB * ((T + 2 * D + 3 + RL - 1) / RL) + 31) / 32 * 32;
+  using TT = Tile<S, R, D, VB, RL, T, NTH>;
   NgsArgs a;
   a.n = n; a.m = m; a.K = K; a.T = T; a.bwd = bwd; a.G = m / VB; a.qb = qb; a.s1 = 0;
   a.b = b; a.x = x; a.y = y; a.ph = ph;
   a.inv_ac = make_sc(3.0 / (8.0 * alpha));
   a.third = make_sc(alpha / 3.0);
-  const int W = T + TT::HL + TT::HR;
-  const size_t BS = (size_t) W * VB * sizeof(S);
-  int nth = VB * ((T + 2 * D + 3 + RL - 1) / RL);
-  nth = (nth + 31) / 32 * 32;
-  if (nth > 128) return (int) cudaErrorInvalidConfiguration;
+  const size_t BS = (size_t) TT::W * VB * sizeof(S);
   const unsigned gx = (unsigned) (a.G * (n / T));
-  cudaFuncSetAttribute(k_node_gs_tile<S, R, D, VB, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int) (12 * BS));
-  cudaFuncSetAttribute(k_node_gs_single<S, R, D, VB, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int) (5 * BS));
-  k_node_gs_single<S, R, D, VB, RL><<<dim3(gx, 1, K), nth, 5 * BS, st>>>(a);
+  cudaFuncSetAttribute(k_node_gs_tile<S, R, D, VB, RL, T, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int) (8 * BS));
+  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 4 * BS, st>>>(a);
   MX_CHECK_LAUNCH();
   const int Q = (n - 2) / 2;
-  k_node_gs_tile<S, R, D, VB, RL><<<dim3(gx, (Q + qb - 1) / qb, K), nth, 12 * BS, st>>>(a);
+  k_node_gs_tile<S, R, D, VB, RL, T, NTH><<<dim3(gx, (Q + qb - 1) / qb, K), NTH, 8 * BS, st>>>(a);
   MX_CHECK_LAUNCH();
   a.s1 = n - 1;
-  k_node_gs_single<S, R, D, VB, RL><<<dim3(gx, 1, K), nth, 5 * BS, st>>>(a);
+  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 4 * BS, st>>>(a);
   MX_CHECK_LAUNCH();
   return 0;
 }
@@ -344,6 +405,7 @@ extern "C" int mxk_node_gs_oop(int n, int m, int K, const double* ph, double alp
                                const void* b, const void* x, void* y, mx_stream s) {
   if (!mxk_node_gs_oop_ok(n, m, prec) || (dir != 0 && dir != 1) || x == y || b == y) return (int) cudaErrorInvalidValue;
   if (((uintptr_t) b | (uintptr_t) x | (uintptr_t) y) & 15) return (int) cudaErrorMisalignedAddress;
-  return run_sweep<float2, float, 8, 4, 5>(n, m, K, ph, alpha, dir, strip_for(n), g_band, b, x, y,
-                                            (cudaStream_t) s);
+  if (strip_for(n) == 128)
+    return run_sweep<float2, float, 8, 4, 5, 128>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
+  return run_sweep<float2, float, 8, 4, 5, 64>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
 }
