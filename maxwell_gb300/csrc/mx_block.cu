@@ -129,6 +129,12 @@ __device__ __forceinline__ void comp_cmac(float* acc, const cx<dd>& a, const cx<
 // ------------------------------------------------------------------
 constexpr int NSTAT = 5;
 
+template <typename R> struct LoAcc { using T = R; };
+template <> struct LoAcc<dd> { using T = float; };
+__device__ __forceinline__ cx<float> lo_c(cx<dd> a) { return mkc(a.re.hi, a.im.hi); }
+__device__ __forceinline__ cx<float> lo_c(cx<float> a) { return a; }
+__device__ __forceinline__ cx<double> lo_c(cx<double> a) { return a; }
+
 template <typename SE, typename SR, typename R>
 __global__ void k_block_residual(int n, int m, int K, const double* __restrict__ ph, KapB<R> kap, Sc axy_s,
                                  Sc sixth, const double* __restrict__ mu, const SE* __restrict__ e,
@@ -145,8 +151,11 @@ __global__ void k_block_residual(int n, int m, int K, const double* __restrict__
   __syncthreads();
   R muv = mu_s[v];
   R four = rc<R>(4.0f);
-  R s_r2 = Real<R>::zero(), s_v2 = Real<R>::zero(), s_ew = Real<R>::zero(), s_ev = Real<R>::zero(),
-    s_ewi = Real<R>::zero();
+  // the Rayleigh quotient's sums in R; the norms and the imaginary check
+  // need a few digits only and take the leading float of a float-float value
+  using RL = typename LoAcc<R>::T;
+  R s_ew = Real<R>::zero(), s_ev = Real<R>::zero();
+  RL s_r2 = 0, s_v2 = 0, s_ewi = 0;
   size_t nsite = (size_t) n * n;
   if (row < rows) {
     for (int site = blockIdx.x * rows + row; site < (int) nsite; site += gridDim.x * rows) {
@@ -170,19 +179,23 @@ __global__ void k_block_residual(int n, int m, int K, const double* __restrict__
         Store<SR, R>::st(rout + L.edge(k, 0, j, i, v), rx);
         Store<SR, R>::st(rout + L.edge(k, 1, j, i, v), ry);
       }
-      s_r2 += rx.re * rx.re + rx.im * rx.im + ry.re * ry.re + ry.im * ry.im;
-      s_v2 += vx.re * vx.re + vx.im * vx.im + vy.re * vy.re + vy.im * vy.im;
+      {
+        const cx<RL> lx = lo_c(rx), ly = lo_c(ry), px = lo_c(vx), py = lo_c(vy), ex = lo_c(x0), ey = lo_c(y0),
+                     qx = lo_c(wx), qy = lo_c(wy);
+        s_r2 += lx.re * lx.re + lx.im * lx.im + ly.re * ly.re + ly.im * ly.im;
+        s_v2 += px.re * px.re + px.im * px.im + py.re * py.re + py.im * py.im;
+        s_ewi += ex.re * qx.im - ex.im * qx.re + ey.re * qy.im - ey.im * qy.re;
+      }
       s_ew += x0.re * wx.re + x0.im * wx.im + y0.re * wy.re + y0.im * wy.im;
       s_ev += x0.re * vx.re + x0.im * vx.im + y0.re * vy.re + y0.im * vy.im;
-      s_ewi += x0.re * wx.im - x0.im * wx.re + y0.re * wy.im - y0.im * wy.re;
     }
   }
   __shared__ double sh[NSTAT][256];
-  sh[0][threadIdx.x] = Real<R>::to_double(s_r2);
-  sh[1][threadIdx.x] = Real<R>::to_double(s_v2);
+  sh[0][threadIdx.x] = (double) s_r2;
+  sh[1][threadIdx.x] = (double) s_v2;
   sh[2][threadIdx.x] = Real<R>::to_double(s_ew);
   sh[3][threadIdx.x] = Real<R>::to_double(s_ev);
-  sh[4][threadIdx.x] = Real<R>::to_double(s_ewi);
+  sh[4][threadIdx.x] = (double) s_ewi;
   __syncthreads();
   if (threadIdx.x < m * NSTAT) {
     int q = threadIdx.x / m, vv = threadIdx.x % m;

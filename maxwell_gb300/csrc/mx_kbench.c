@@ -307,6 +307,10 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
       if(mxk_node_gs_oop_ok(n, m, MX_C64))
         TIME("node_gs_tiled_c64", 3 * V8 * s8, 3,
              mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
+      mxk_node_gs_oop_shape(64, 16);
+      if(mxk_node_gs_oop_ok(n, m, MX_C64))
+        TIME("node_gs_tiled64_c64", 3 * V8 * s8, 3,
+             mxk_node_gs_oop(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, nd, st));
       mxk_node_gs_oop_shape(s0, b0);
     }
     TIME("node_restrict_c64", (V8 + 2 * V8 / 4) * s8, 1,

@@ -30,9 +30,8 @@
 // (t, s) = (i, j), backward (t, s) = (n-1-i, n-1-j) with conjugate phases,
 // so one code path serves both directions.
 //
-// Each step of a CTA stages, by cp.async one step ahead, the two next old
-// rows (b goes to registers one phase ahead); a step is four phases
-// separated by barriers:
+// Each step of a CTA stages, by cp.async P steps ahead, its two next old
+// rows and its two b rows; a step is four phases separated by barriers:
 // betas of the odd row (runs of RL positions per thread, a sliding window
 // over the neighbour rows), its truncated prefix sums (Horner over the D
 // betas before a run, then the recurrence), the betas of the even row, its
@@ -49,8 +48,8 @@ __device__ __forceinline__ void cpa16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cpa_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cpa_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 struct NgsArgs {
   int n, m, K, T, bwd;
@@ -131,14 +130,6 @@ struct Tile {
   __device__ __forceinline__ cx<R> L(const S* buf, int u, int v) const {
     return Store<S, R>::ld(buf + (size_t) (u - base) * VB + v);
   }
-  // b of the row s at position u, through the seam
-  __device__ __forceinline__ cx<R> ldb(const S* B, int s, int u, int v) const {
-    const int c = canon(u);
-    cx<R> z = Store<S, R>::ld(B + row(s) + (size_t) col(c) * m + v);
-    if (u < 0) z = pl * z;
-    else if (u >= n) z = pr * z;
-    return z;
-  }
   // the run [p0, p0+len) of task `task` over [ua, ub); fast: a full run
   // whose betas read canonical positions 1..n-2 only
   __device__ __forceinline__ bool run_of(int task, int ua, int ub, int& v, int& p0, int& len) const {
@@ -147,27 +138,16 @@ struct Tile {
     len = ub - p0 < RL ? ub - p0 : RL;
     return len == RL && p0 - 1 >= 1 && p0 + RL + 1 <= n - 2;
   }
-  // right-hand side of a fast beta run, into registers
-  __device__ __forceinline__ void loadb(int task, int ua, int ub, const S* B, int s, cx<R> (&bv)[RL]) const {
-    int v, p0, len;
-    if (task >= ((ub - ua + RL - 1) / RL) * VB || !run_of(task, ua, ub, v, p0, len)) return;
-    const S* bp = B + row(s) + (size_t) col(p0) * m + v;
-    const int st = bwd ? -m : m;
-#pragma unroll
-    for (int q = 0; q < RL; q++) bv[q] = Store<S, R>::ld(bp + q * st);
-  }
-
-  // betas of positions [ua, ub) of the row s: below / above are the rows
-  // s-1 and s+1 (old or new), own the row's old values; b in bv for a fast
-  // run, else read here
-  __device__ void betas(int task, int ua, int ub, const S* below, const S* above, const S* own, const S* B,
-                        int s, const cx<R> (&bv)[RL], S* beta) const {
+  // betas of positions [ua, ub) of a row: below / above are the rows s-1 and
+  // s+1 (old or new), own the row's old values, bb its right-hand side
+  __device__ void betas(int task, int ua, int ub, const S* below, const S* above, const S* own, const S* bb,
+                        S* beta) const {
     int v, p0, len;
     if (task >= ((ub - ua + RL - 1) / RL) * VB) return;
     const R eighth = rc<R>(0.125f);
     if (run_of(task, ua, ub, v, p0, len)) {
       const int o = (p0 - base) * VB + v;
-      const S *pb_ = below + o, *pa_ = above + o, *po = own + o;
+      const S *pb_ = below + o, *pa_ = above + o, *po = own + o, *pr_ = bb + o;
       S* pz = beta + o;
       cx<R> cm = Store<S, R>::ld(pb_ - VB) + Store<S, R>::ld(pa_ - VB);
       cx<R> c0 = Store<S, R>::ld(pb_) + Store<S, R>::ld(pa_);
@@ -175,7 +155,8 @@ struct Tile {
       for (int q = 0; q < RL; q++) {
         const cx<R> cp = Store<S, R>::ld(pb_ + (q + 1) * VB) + Store<S, R>::ld(pa_ + (q + 1) * VB);
         const cx<R> nb = (cm + c0) + cp;
-        Store<S, R>::st(pz + q * VB, scal(inv_ac, bv[q] + scal(third, Store<S, R>::ld(po + (q + 1) * VB) + nb)));
+        Store<S, R>::st(pz + q * VB, scal(inv_ac, Store<S, R>::ld(pr_ + q * VB)
+                                                      + scal(third, Store<S, R>::ld(po + (q + 1) * VB) + nb)));
         cm = c0;
         c0 = cp;
       }
@@ -190,12 +171,12 @@ struct Tile {
       if (c == n - 1) {
         // the new value at the cut u+1, from old values around it
         const cx<R> cpp = L(below, u + 2, v) + L(above, u + 2, v);
-        nxt = scal(inv_ac, ldb(B, s, u + 1, v) + scal(third, L(own, u + 2, v) + ((c0 + cp) + cpp)))
+        nxt = scal(inv_ac, L(bb, u + 1, v) + scal(third, L(own, u + 2, v) + ((c0 + cp) + cpp)))
               + scal(eighth, L(own, u, v));
       } else {
         nxt = L(own, u + 1, v);
       }
-      cx<R> be = scal(inv_ac, ldb(B, s, u, v) + scal(third, nxt + ((cm + c0) + cp)));
+      cx<R> be = scal(inv_ac, L(bb, u, v) + scal(third, nxt + ((cm + c0) + cp)));
       if (c == 0) be = be + scal(eighth, L(own, u - 1, v));
       Store<S, R>::st(beta + (size_t) (u - base) * VB + v, be);
       cm = c0;
@@ -240,10 +221,13 @@ struct Tile {
   }
 };
 
-// launch 2: rows 1..n-2, grid (G x strips, bands, K)
-template <typename S, typename R, int D, int VB, int RL, int T, int NTH>
-__global__ void __launch_bounds__(NTH, 5) k_node_gs_tile(NgsArgs a) {
+// launch 2: rows 1..n-2, grid (G x strips, bands, K).  The copies run P
+// steps ahead: rows in a ring of 2P+3 slots (slot s mod 2P+3), the b rows of
+// a step's odd and even row in P+1 pairs of slots.
+template <typename S, typename R, int D, int VB, int RL, int T, int NTH, int P>
+__global__ void __launch_bounds__(NTH) k_node_gs_tile(NgsArgs a) {
   using TT = Tile<S, R, D, VB, RL, T, NTH>;
+  constexpr int NO = 2 * P + 3, NB2 = P + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int tid = threadIdx.x;
   const TT t(a, blockIdx.x / a.G, blockIdx.x % a.G, blockIdx.z, tid);
@@ -252,9 +236,10 @@ __global__ void __launch_bounds__(NTH, 5) k_node_gs_tile(NgsArgs a) {
   if (q0 >= Q) return;
   constexpr int BS = TT::W * VB;
   S* sm = reinterpret_cast<S*>(smraw);
-  S* old = sm;                 // 5 rows, slot s % 5
-  S* odd = sm + 5 * BS;        // 2 rows: step & 1
-  S* beta = sm + 7 * BS;
+  S* old = sm;                    // NO rows
+  S* bsm = sm + NO * BS;          // NB2 pairs (odd, even)
+  S* odd = bsm + 2 * NB2 * BS;    // 2 rows: step & 1
+  S* beta = odd + 2 * BS;
   const S* X = reinterpret_cast<const S*>(a.x);
   const S* B = reinterpret_cast<const S*>(a.b);
   S* Y = reinterpret_cast<S*>(a.y);
@@ -263,54 +248,59 @@ __global__ void __launch_bounds__(NTH, 5) k_node_gs_tile(NgsArgs a) {
   // the phases' ranges: odd betas, odd new values, even betas / new values
   const int ob0 = t0 - 2 * D - 1, ob1 = t0 + T + 2, on0 = t0 - D - 1, on1 = t0 + T + 2;
   const int eb0 = t0 - D, eb1 = t0 + T;
-  cx<R> bodd[RL], bev[RL];
-
-  // prologue: the rows and b of the first odd row (row 0 comes from y)
-  {
-    const int o = 2 * q0 + 1;
-    for (int s = o - 1; s <= o + 1; s++) t.stage(old + (s % 5) * BS, s == 0 ? Y : X, s);
+  // what step j needs beyond the rows of step j-1 (row 0 comes from y)
+  auto stage_step = [&](int j) {
+    const int o = 2 * (q0 + j) + 1;
+    S* bp = bsm + (j % NB2) * 2 * BS;
+    if (j == 0) {
+      for (int s = o - 1; s <= o + 1; s++) t.stage(old + (s % NO) * BS, s == 0 ? Y : X, s);
+    } else {
+      t.stage(old + (o % NO) * BS, X, o);
+      if (o + 1 <= n - 1) t.stage(old + ((o + 1) % NO) * BS, X, o + 1);
+      t.stage(bp + BS, B, o - 1);
+    }
+    if (o <= n - 2) t.stage(bp, B, o);
+  };
+#pragma unroll
+  for (int j = 0; j < P; j++) {
+    if (j < nsteps) stage_step(j);
     cpa_commit();
-    t.loadb(tid, ob0, ob1, B, o, bodd);
   }
   for (int i = 0; i < nsteps; i++) {
     const int o = 2 * (q0 + i) + 1, e = o - 1;
-    // stage rows o+2 and o+3 for step i+1, into slots step i-1 used last
-    if (i + 1 < nsteps) {
-      t.stage(old + ((o + 2) % 5) * BS, X, o + 2);
-      if (o + 3 <= n - 1) t.stage(old + ((o + 3) % 5) * BS, X, o + 3);
-    }
+    if (i + P < nsteps) stage_step(i + P);   // into slots step i-1 used last
     cpa_commit();
-    if (i > 0) t.loadb(tid, eb0, eb1, B, e, bev);
-    cpa_wait1();
+    cpa_wait<P>();
     __syncthreads();
+    S* bo = bsm + (i % NB2) * 2 * BS;
     if (edge) {
-      if (i == 0) t.fix(old + ((o - 1) % 5) * BS, o - 1, tid);
-      t.fix(old + (o % 5) * BS, o, tid);
-      if (o + 1 <= n - 1) t.fix(old + ((o + 1) % 5) * BS, o + 1, tid);
+      if (i == 0) t.fix(old + ((o - 1) % NO) * BS, o - 1, tid);
+      t.fix(old + (o % NO) * BS, o, tid);
+      if (o + 1 <= n - 1) t.fix(old + ((o + 1) % NO) * BS, o + 1, tid);
+      if (o <= n - 2) t.fix(bo, o, tid);
+      if (i > 0) t.fix(bo + BS, e, tid);
       __syncthreads();
     }
     const S* above;
     if (o <= n - 2) {
       S* on = odd + (i & 1) * BS;
-      t.betas(tid, ob0, ob1, old + ((o - 1) % 5) * BS, old + ((o + 1) % 5) * BS, old + (o % 5) * BS, B, o, bodd,
-              beta);
+      t.betas(tid, ob0, ob1, old + ((o - 1) % NO) * BS, old + ((o + 1) % NO) * BS, old + (o % NO) * BS, bo, beta);
       __syncthreads();
       // the odd row of the next band is recomputed here, not written
       t.prefix(tid, on0, on1, beta, on, i < q1 - q0 ? Y + t.row(o) : nullptr);
       __syncthreads();
       above = on;
     } else {
-      above = old + (o % 5) * BS;   // the even row n-2 reads the old row n-1
+      above = old + (o % NO) * BS;   // the even row n-2 reads the old row n-1
     }
-    if (i + 1 < nsteps && o + 2 <= n - 2) t.loadb(tid, ob0, ob1, B, o + 2, bodd);
     if (i > 0) {
-      t.betas(tid, eb0, eb1, odd + ((i - 1) & 1) * BS, above, old + (e % 5) * BS, B, e, bev, beta);
+      t.betas(tid, eb0, eb1, odd + ((i - 1) & 1) * BS, above, old + (e % NO) * BS, bo + BS, beta);
       __syncthreads();
       t.prefix(tid, eb0 + D, eb1, beta, nullptr, Y + t.row(e));
     }
     __syncthreads();
   }
-  cpa_wait0();
+  cpa_wait<0>();
 }
 
 // launches 1 and 3: the single row s1 (0 or n-1 in sweep order), grid
@@ -326,26 +316,27 @@ __global__ void __launch_bounds__(NTH) k_node_gs_single(NgsArgs a) {
   constexpr int BS = TT::W * VB;
   S* sm = reinterpret_cast<S*>(smraw);
   const S* X = reinterpret_cast<const S*>(a.x);
-  const S* B = reinterpret_cast<const S*>(a.b);
   const S* nbr = s == 0 ? X : reinterpret_cast<const S*>(a.y);
-  cx<R> bv[RL];
   t.stage(sm, nbr, s - 1);
   t.stage(sm + BS, nbr, s + 1);
   t.stage(sm + 2 * BS, X, s);
+  t.stage(sm + 3 * BS, reinterpret_cast<const S*>(a.b), s);
   cpa_commit();
-  t.loadb(tid, t0 - D, t0 + T, B, s, bv);
-  cpa_wait0();
+  cpa_wait<0>();
   __syncthreads();
   t.fix(sm, s - 1, tid);
   t.fix(sm + BS, s + 1, tid);
-  if (t.edge()) t.fix(sm + 2 * BS, s, tid);
+  if (t.edge()) {
+    t.fix(sm + 2 * BS, s, tid);
+    t.fix(sm + 3 * BS, s, tid);
+  }
   __syncthreads();
-  t.betas(tid, t0 - D, t0 + T, sm, sm + BS, sm + 2 * BS, B, s, bv, sm + 3 * BS);
+  t.betas(tid, t0 - D, t0 + T, sm, sm + BS, sm + 2 * BS, sm + 3 * BS, sm + 4 * BS);
   __syncthreads();
-  t.prefix(tid, t0, t0 + T, sm + 3 * BS, nullptr, reinterpret_cast<S*>(a.y) + t.row(s));
+  t.prefix(tid, t0, t0 + T, sm + 4 * BS, nullptr, reinterpret_cast<S*>(a.y) + t.row(s));
 }
 
-template <typename S, typename R, int D, int VB, int RL, int T>
+template <typename S, typename R, int D, int VB, int RL, int T, int P>
 int run_sweep(int n, int m, int K, const double* ph, double alpha, int bwd, int qb, const void* b, const void* x,
               void* y, cudaStream_t st) {
   // one run per thread in every phase: the longest phase has T + 2D + 3 positions
@@ -358,15 +349,16 @@ int run_sweep(int n, int m, int K, const double* ph, double alpha, int bwd, int 
   a.third = make_sc(alpha / 3.0);
   const size_t BS = (size_t) TT::W * VB * sizeof(S);
   const unsigned gx = (unsigned) (a.G * (n / T));
-  cudaFuncSetAttribute(k_node_gs_tile<S, R, D, VB, RL, T, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int) (8 * BS));
-  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 4 * BS, st>>>(a);
+  const size_t tile_smem = (size_t) (2 * P + 3 + 2 * (P + 1) + 3) * BS;
+  cudaFuncSetAttribute(k_node_gs_tile<S, R, D, VB, RL, T, NTH, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int) tile_smem);
+  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 5 * BS, st>>>(a);
   MX_CHECK_LAUNCH();
   const int Q = (n - 2) / 2;
-  k_node_gs_tile<S, R, D, VB, RL, T, NTH><<<dim3(gx, (Q + qb - 1) / qb, K), NTH, 8 * BS, st>>>(a);
+  k_node_gs_tile<S, R, D, VB, RL, T, NTH, P><<<dim3(gx, (Q + qb - 1) / qb, K), NTH, tile_smem, st>>>(a);
   MX_CHECK_LAUNCH();
   a.s1 = n - 1;
-  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 4 * BS, st>>>(a);
+  k_node_gs_single<S, R, D, VB, RL, T, NTH><<<dim3(gx, 1, K), NTH, 5 * BS, st>>>(a);
   MX_CHECK_LAUNCH();
   return 0;
 }
@@ -406,6 +398,6 @@ extern "C" int mxk_node_gs_oop(int n, int m, int K, const double* ph, double alp
   if (!mxk_node_gs_oop_ok(n, m, prec) || (dir != 0 && dir != 1) || x == y || b == y) return (int) cudaErrorInvalidValue;
   if (((uintptr_t) b | (uintptr_t) x | (uintptr_t) y) & 15) return (int) cudaErrorMisalignedAddress;
   if (strip_for(n) == 128)
-    return run_sweep<float2, float, 8, 4, 5, 128>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
-  return run_sweep<float2, float, 8, 4, 5, 64>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
+    return run_sweep<float2, float, 8, 4, 5, 128, 2>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
+  return run_sweep<float2, float, 8, 4, 5, 64, 3>(n, m, K, ph, alpha, dir, g_band, b, x, y, (cudaStream_t) s);
 }

@@ -50,7 +50,8 @@ def test_continuity_matches_oracle(oracle, golden, continuity):
     # phases, do not see it).  So every adjusted vector equals the oracle's
     # up to one unit factor, and the GPU's own vectors meet the rule itself:
     # e_i^H M guess_i real and non-negative, guess_i the previous point's
-    # vector (or 2 e_i(l-1) - e_i(l-2) away from corners)
+    # vector (or 2 e_i(l-1) - e_i(l-2) away from corners), wherever that
+    # overlap is not rounding noise
     scale = np.abs(v_o).max()
     for l in range(nk):
         for i in range(m):
@@ -63,6 +64,7 @@ def test_continuity_matches_oracle(oracle, golden, continuity):
                 prev2 = adj[l - 2, i] if l > 1 else np.zeros_like(adj[0, i])
                 guess = adj[l - 1, i] if vertex[l - 1] else 2 * adj[l - 1, i] - prev2
                 p = oracle.massprod_edge(n, *fac[l], guess, adj[l, i])
-                assert abs(p.imag) <= 1e-9 * abs(p) and p.real >= 0, (l, i, p)
+                if abs(p) > 1e-6:   # else a band change: the overlap, and the phase, is noise
+                    assert abs(p.imag) <= 1e-9 * abs(p) and p.real >= 0, (l, i, p)
     if continuity == "n":
         assert np.array_equal(adj, raw)
