@@ -438,8 +438,9 @@ def run_config5(args):
     16 x 16 checkerboard of eps in {1, 4, 8.9, 12}, 8 k-points at the
     high-symmetry corners and edge midpoints (Gamma, X, Y, M, the midpoints of
     Gamma-X, Gamma-Y, Gamma-M and X-M), 24 pairs with block 32 via LOBPCG,
-    9 multigrid levels 2048 .. 8 in FP32 complex, relative residual 1e-9,
-    then one refinement sweep and the FP64 residual check.  Solved in two
+    9 multigrid levels 2048 .. 8 in FP32 complex, the eigenvector block in
+    FP64 (precision 2), relative residual 1e-9, then one refinement sweep and
+    the FP64 residual check.  Solved in two
     batches of 4 k-points (about 120 GB on the device each).  Not the
     headline metric: one JSON line."""
     import maxwell_gb300 as mx
@@ -450,7 +451,9 @@ def run_config5(args):
     pi = np.pi
     kpts = np.array([(0, 0), (pi, 0), (0, pi), (pi, pi), (pi / 2, 0), (0, pi / 2), (pi / 2, pi / 2), (pi, pi / 2)])
     fac = factors_of(kpts)
-    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, max_nested=MAX_NESTED, max_steps=120,
+    # FP64 eigenvector block (FP32 multigrid and search blocks): at 2048^2 the
+    # float-float block's residual floor, ||A|| 2^-48 / lambda, lies above 1e-9
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=2, max_nested=MAX_NESTED, max_steps=120,
                   wave=4, relative=1, tol=tol, refine=1)
     ms_all, lams, steps_all, res_max, fp_max, launches = 0.0, [], [], 0.0, 0.0, 0
     for b in range(2):
@@ -468,7 +471,8 @@ def run_config5(args):
                       "gpu_launches": launches, "lambda_first": [float(v) for v in np.concatenate(lams)[:, 0]],
                       "config": {"workload": "2048^2, 16x16 checkerboard eps {1,4,8.9,12} seed 0, 8 k-points "
                                              "(Gamma X Y M and midpoints), 24 pairs block 32, LOBPCG, 9 levels, "
-                                             "relative residual 1e-9 + refinement sweep + FP64 check",
+                                             "FP64 eigenvectors + FP32 multigrid, relative residual 1e-9 + "
+                                             "refinement sweep + FP64 check",
                                  "batches": "2 x 4 k-points"}}), flush=True)
 
 
@@ -477,8 +481,8 @@ def run_surface(args):
     of radius 0.15 centred at (0.25|0.75, 0.25|0.75), a 32 x 32 k-grid over
     [-pi, pi]^2 solved in waves of --wave k-points (64: two rows), every wave
     after the first started as --extrapolation says (by default from the
-    Rayleigh-Ritz extrapolation over the same slots of the three waves before
-    it), 12 pairs with block 16 via LOBPCG, mixed
+    eigenvectors of the same slots of the wave before it), 12 pairs with
+    block 16 via LOBPCG, mixed
     precision, relative residual 1e-8.  Not the headline metric: one JSON
     line of k-points/s."""
     import maxwell_gb300 as mx
@@ -525,7 +529,7 @@ def main():
     ap.add_argument("--surface", action="store_true", help="the full-zone surface workload instead of the metric")
     ap.add_argument("--config5", action="store_true", help="the 2048^2 block-32 workload instead of the metric")
     ap.add_argument("--wave", type=int, default=64, help="k-points per wave of the --surface workload")
-    ap.add_argument("--extrapolation", default="2", choices=["n", "1", "2", "c"],
+    ap.add_argument("--extrapolation", default="n", choices=["n", "1", "2", "c"],
                     help="start of the --surface workload's later waves: warm from the waves before "
                          "('n', or Rayleigh-Ritz over 2 or 3 waves '1', '2') or cold ('c')")
     ap.add_argument("--autotune", action="store_true",

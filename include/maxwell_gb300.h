@@ -260,7 +260,11 @@ typedef struct {
   int n0, L;             /* coarse intervals, refinement levels (n = n0 << L) */
   int ieigs, m;          /* wanted pairs, block size (m <= 32) */
   int method;            /* 0 block PINVIT + Ritz (exp_bloch2d), 1 LOBPCG */
-  int precision;         /* 0 plain FP64, 1 mixed (FP32 multigrid, float-float eigenvectors) */
+  int precision;         /* 0 plain FP64, 1 mixed (FP32 multigrid, float-float eigenvectors),
+                          * 2 mixed with FP64 eigenvectors (FP32 multigrid and search
+                          * blocks): the float-float block's residual floor, about
+                          * ||A|| 2^-48 / lambda relative, grows with n^2 (near 1e-9 at
+                          * 1024^2); FP64 lowers it 32-fold */
   int max_nested;        /* block steps per level of the nested iteration */
   int max_steps;         /* block steps at the finest level */
   int prec_steps;        /* edge V-cycles per preconditioner application */

@@ -757,7 +757,7 @@ __device__ __forceinline__ void tri_index(int e, int& i, int& j) {
   j = e - i * (i + 1) / 2;
 }
 
-__global__ void __launch_bounds__(G2T, 1) k_block_gram_mixed(GramArgs a) {
+__global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
   const int k = blockIdx.y, chunk = blockIdx.x;
   const int n = a.n, m = a.m, ns = a.ns, nb = a.nb;
   const int nent = ns * (ns + 1) / 2, ment = m * (m + 1) / 2;

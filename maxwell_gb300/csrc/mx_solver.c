@@ -181,6 +181,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   double *kk[MAXL];
   if(o->L < 0 || o->L >= MAXL - 1 || o->n0 < 4 || (o->n0 & 1) || o->m < 1 || o->m > 32
      || o->ieigs < 1 || o->ieigs > o->m || o->wave < 1 || o->smoother < 0 || o->smoother > 2
+     || o->precision < 0 || o->precision > 2
      || (o->extrapolation != 0 && o->extrapolation != 'n' && o->extrapolation != '1' && o->extrapolation != '2'
          && o->extrapolation != 'c'))
     return 0;
@@ -189,7 +190,11 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
   s->order = o->extrapolation == '2' ? 3 : o->extrapolation == '1' ? 2 : 1;
   if(cudaGetDevice(&s->device) != cudaSuccess) { free(s); return 0; }
   s->n0 = o->n0; s->L = o->L; s->m = m = o->m; s->K = K = o->wave;
-  s->pe = o->precision ? MX_CDD : MX_C128;
+  /* precision 0: everything FP64; 1: float-float eigenvector block, FP32
+   * multigrid and search blocks; 2: FP64 eigenvector block, FP32 multigrid
+   * and search blocks (for residuals below the float-float floor, about
+   * ||A|| 2^-48 / lambda relative, which grows with n^2) */
+  s->pe = o->precision == 1 ? MX_CDD : MX_C128;
   s->pg = o->precision ? MX_C64 : MX_C128;
   es_g = mxk_elem_size(s->pg);
   es_e = mxk_elem_size(s->pe);
@@ -636,7 +641,7 @@ static int ritz_body(mxg_solver *s, int l)
   const void *const *pp = s->rb.pp;
   /* the residual of E sits in b[l] (written by residual()) with the Ritz
    * values mu; the mixed solver forms the E-to-search-block entries from it */
-  const void *rr = (s->pe == MX_CDD && nb > 1) ? s->b[l] : 0;
+  const void *rr = (s->pg == MX_C64 && nb > 1) ? s->b[l] : 0;
   int tm = s->timing && l == s->L && nb > 1, on, b;
   double gbytes = 12.0 * s->n[l] * s->n[l];   /* kappa as float and float-float pair */
   for(b = 0; b < nb; b++) gbytes += (double) elen(s, l) * mxk_elem_size(pr[b]);

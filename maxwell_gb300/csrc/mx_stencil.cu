@@ -1467,6 +1467,7 @@ extern "C" int mxk_gradient(int n, int m, int K, const double* ph, double alpha,
   else if (pv == MX_C128 && pe == MX_C128) MX_G(double2, double2, double);
   else if (pv == MX_C64 && pe == MX_CDD) MX_G(float2, cdd, dd);
   else if (pv == MX_CDD && pe == MX_CDD) MX_G(cdd, cdd, dd);
+  else if (pv == MX_C64 && pe == MX_C128) MX_G(float2, double2, double);
   else return (int) cudaErrorInvalidValue;
 #undef MX_G
   MX_CHECK_LAUNCH();
@@ -1487,6 +1488,7 @@ extern "C" int mxk_adjgradient(int n, int m, int K, const double* ph, double alp
   // cancellation: it is formed in float-float and only then rounded to c64
   else if (pe == MX_CDD && pv == MX_C64) MX_AG(cdd, float2, dd);
   else if (pe == MX_CDD && pv == MX_CDD) MX_AG(cdd, cdd, dd);
+  else if (pe == MX_C128 && pv == MX_C64) MX_AG(double2, float2, double);
   else return (int) cudaErrorInvalidValue;
 #undef MX_AG
   MX_CHECK_LAUNCH();

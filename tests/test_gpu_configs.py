@@ -120,3 +120,25 @@ def test_large_block_matches_oracle(oracle, m, ie):
                                             max_steps=80, tol=1e-10, relative=1, extrapolation="n", wave=1)
     assert st == 0
     assert (np.abs(lam[:, :ie] - lam_o[:, :ie]) / lam_o[:, :ie]).max() < 1e-8
+
+
+def test_fp64_block_below_float_float_floor():
+    """Precision 2 (FP64 eigenvector block, FP32 multigrid and search blocks)
+    reaches a relative residual of 1e-10 at 512^2, below the float-float
+    block's floor there (||A|| 2^-48 / lambda, a few 1e-10), with the FP64
+    recheck agreeing, and its eigenvalues agree with the float-float
+    solver's at that solver's own accuracy."""
+    import bench
+    n0, L = 8, 6
+    kap = bench.checkerboard_kappa(n0 << L)
+    fac = bench.factors_of(np.array([(np.pi / 2, np.pi / 2)]))
+    s2 = mx.Solver(kap, n0=n0, L=L, ieigs=12, m=16, method=1, precision=2, max_nested=5, max_steps=60, wave=1,
+                   relative=1, tol=1e-10)
+    lam2, st2, res2 = s2.solve(fac)
+    assert res2[:, :12].max() <= 1e-10, (st2, res2[:, :12].max())
+    assert s2.check_fp64()[:, :12].max() <= 2e-10
+    s1 = mx.Solver(kap, n0=n0, L=L, ieigs=12, m=16, method=1, precision=1, max_nested=5, max_steps=60, wave=1,
+                   relative=1, tol=1e-9)
+    lam1, st1, res1 = s1.solve(fac)
+    assert res1[:, :12].max() <= 1e-9
+    assert np.abs(lam1[:, :12] - lam2[:, :12]).max() / np.abs(lam2[:, :12]).max() < 1e-9
