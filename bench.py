@@ -351,7 +351,7 @@ def run_ours(args):
         "roofline": roof("node_gs", "k_node_gs_warp + k_node_gs_row (node Gauss-Seidel of the gradient "
                                     "lifting, finest level)", "one node GS sweep (4 launches)",
                          TRAFFIC_32K["node_gs"]),
-        "roofline_more": [roof("gram", "k_block_gram_mixed + k_gram_reduce (Gram matrices of [E X P])",
+        "roofline_more": [roof("gram", "k_block_gram_split + k_gram_reduce (Gram matrices of [E X P])",
                                "one Gram of the Ritz step", TRAFFIC_32K["gram"]),
                           roof("afw", "k_edge_gs_rowpair (AFW sweep in four colours, finest level)",
                                "one AFW sweep (2 row-pair launches)", TRAFFIC_32K["afw"])],

@@ -725,31 +725,6 @@ extern "C" int mxk_block_residual(int n, int m, int K, const double* ph, mxk_kap
   return 0;
 }
 
-// ------------------------------------------------------------------
-// Gram matrices of the mixed solver: column block 0 is the float-float
-// eigenvector block E (m <= 16 columns), blocks 1.. are c64, and the
-// entries between a c64 column s_i and an E column e_j take the residual
-// form theta_j s_i^H M e_j + s_i^H r_j.  One CTA of G2T threads takes a chunk
-// of sites of one k-point, in tiles of G2S sites staged in shared memory:
-//   threads 0..287   the FP32 entries, one 2x2 tile of entries per thread:
-//                    the 8x8 tiles of each block pair bi > bj (threads
-//                    0..191) and the lower-triangle tiles of the diagonal
-//                    blocks bi = bj >= 1 (threads 192..263); a tile loads
-//                    its two row and two column operands once per site and
-//                    accumulates the four entries by FMA;
-//   threads 288..559 the E-E entries (lower triangle, <= 136), two threads
-//                    per entry on alternate sites of a tile, accumulated as
-//                    compensated FP32 sums of exact products (TwoProd by
-//                    FMA, TwoSum; the low parts of E enter through the
-//                    cross products), which carry about twice the FP32
-//                    precision like float-float arithmetic at half its cost.
-// Partial sums per CTA go to scratch in the layout of k_block_gram.
-// ------------------------------------------------------------------
-constexpr int G2F = 288;         // FP32 role: 9 warps, 264 tiles
-constexpr int G2T = G2F + 288;   // + E-E role: 9 warps, 272 threads used
-constexpr int G2S = 16;          // sites per tile
-constexpr int G2MAXO = 3;        // off-diagonal block pairs (nb <= 3)
-
 __device__ __forceinline__ void tri_index(int e, int& i, int& j) {
   i = (int) ((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
   while (i * (i + 1) / 2 > e) i--;
@@ -757,227 +732,291 @@ __device__ __forceinline__ void tri_index(int e, int& i, int& j) {
   j = e - i * (i + 1) / 2;
 }
 
-__global__ void __launch_bounds__(G2T, 2) k_block_gram_mixed(GramArgs a) {
-  const int k = blockIdx.y, chunk = blockIdx.x;
-  const int n = a.n, m = a.m, ns = a.ns, nb = a.nb;
-  const int nent = ns * (ns + 1) / 2, ment = m * (m + 1) / 2;
-  const int tid = threadIdx.x;
-  extern __shared__ float sm2[];
-  cx<float>* fi = reinterpret_cast<cx<float>*>(sm2);        // [G2S][3][ns]: c, x, y
-  cx<float>* fj = fi + G2S * 3 * ns;                        // [G2S][3][ns]: kappa c, Mx, My
-  cx<float>* fr = fj + G2S * 3 * ns;                        // [G2S][2][m]: rx, ry
-  cx<dd>* di = reinterpret_cast<cx<dd>*>(fr + G2S * 2 * m);  // [G2S][3][m]
-  cx<dd>* dj = di + G2S * 3 * m;                             // [G2S][3][m]
-  Lay L{n, m, a.K};
-  const dd sixth_d = sget<dd>(a.sixth), four_d = rc<dd>(4.0f);
-  const float sixth_f = a.sixth.hi;
-  const bool use_r = a.resid != nullptr;
+// ------------------------------------------------------------------
+// Gram matrices of the mixed solver: column block 0 is the float-float
+// eigenvector block E (m <= 16 columns), blocks 1.. are c64, and the
+// entries between a c64 column s_i and an E column e_j take the residual
+// form theta_j s_i^H M e_j + s_i^H r_j (r_j the float-float residual rounded
+// to c64), which keeps the cancellation of s_i^H (A+M) e_j out of FP32.  The
+// two kinds of entries are separate CTAs of one launch (grid z = 0: FP32
+// entries, z = 1: E-E entries), each staging only what its entries read:
+//   FP32 CTAs  every entry with a c64 column: the 4x2 tiles of the block
+//              pairs (1,0), (2,0), (2,1) and the lower-triangle tiles of
+//              (1,1), (2,2); a tile's two threads take alternate sites of a
+//              32-site tile and meet by a shuffle at the end.  Per site a
+//              tile loads 4 row and 2 column operands for 8 entries.
+//   E-E CTAs   the lower-triangle 2x2 tiles of the E block as compensated
+//              FP32 sums of exact products; eight threads per tile take every
+//              eighth site and meet by shuffles (in FP64) at the end.
+// The E-E sums carry about twice the FP32 precision (TwoProd by FMA, TwoSum;
+// the low parts of E enter through the cross products), like float-float
+// arithmetic at half its cost.  Partial sums per CTA go to scratch in the
+// layout of k_block_gram.
+// ------------------------------------------------------------------
+constexpr int GS_T = 288;   // threads per CTA
+constexpr int GS_S = 32;    // sites per tile
 
-  // ---- roles ----
-  // FP32 tile of this thread: block row tbi, block column tbj, tile (ti, tj)
-  // of the block's 8x8 tiles; rows r0, r1 and columns c0, c1 of the Gram
-  // matrix (a row or column past the block repeats the first, unused)
-  constexpr int PBI[G2MAXO] = {1, 2, 2}, PBJ[G2MAXO] = {0, 0, 1};
-  int tbi = nb, tbj = 0, ti = 0, tj = 0;
-  if (tid < 64 * G2MAXO) {
-    tbi = PBI[tid >> 6];
-    tbj = PBJ[tid >> 6];
-    ti = (tid & 63) >> 3;
-    tj = tid & 7;
-  } else if (tid < 64 * G2MAXO + 72) {
-    const int e = tid - 64 * G2MAXO;
-    tbi = tbj = 1 + e / 36;
-    tri_index(e % 36, ti, tj);
+// FP32 tiles are 4 rows x 2 columns: 32 per full block pair (1,0), (2,0),
+// (2,1) with bi < nb, then 20 per diagonal block (1,1), (2,2) (the tiles with
+// an entry on or below the diagonal: 2, 4, 6, 8 column tiles for row tiles 0..3)
+__device__ __forceinline__ void gs_tile_f(int q, int nb, int& bi, int& bj, int& ti, int& tj) {
+  const int nfull = nb == 3 ? 3 : (nb == 2 ? 1 : 0);
+  if (q < 32 * nfull) {
+    const int pr = q >> 5, r = q & 31;
+    bi = pr == 0 ? 1 : 2;
+    bj = pr == 2 ? 1 : 0;
+    ti = r >> 3;
+    tj = r & 7;
+  } else {
+    const int r = q - 32 * nfull, rr = r % 20;
+    bi = bj = 1 + r / 20;
+    ti = rr < 2 ? 0 : (rr < 6 ? 1 : (rr < 12 ? 2 : 3));
+    tj = rr - (ti == 0 ? 0 : (ti == 1 ? 2 : (ti == 2 ? 6 : 12)));
   }
-  const bool ftile = tbi < nb && 2 * ti < m && 2 * tj < m;
-  const bool rmode = use_r && tbj == 0;
-  const int r0 = tbi * m + 2 * ti, c0 = tbj * m + 2 * tj;
-  const int r1 = 2 * ti + 1 < m ? r0 + 1 : r0, c1 = 2 * tj + 1 < m ? c0 + 1 : c0;
-  // accumulators: an FP32 tile uses all of acc (entry (r_a, c_b) at
-  // 4 (2a + b): A re, A im, M re, M im), E-E threads the first 8 (A, M as
-  // compensated sums)
-  float acc[16];
-  const int u = tid - G2F;
-  const bool drole = u >= 0 && (u >> 1) < ment;
-  const int half = u & 1;
-  int ei = 0, ej = 0;
-  if (drole) tri_index(u >> 1, ei, ej);
-#pragma unroll
-  for (int q = 0; q < 16; q++) acc[q] = 0.f;
-  float* const eacc_a = acc;
-  float* const eacc_m = acc + 4;
+}
 
+__global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
+  const int k = blockIdx.y, chunk = blockIdx.x, role = blockIdx.z;
+  const int n = a.n, m = a.m, ns = a.ns, nb = a.nb;
+  const int nent = ns * (ns + 1) / 2;
+  const int tid = threadIdx.x;
+  extern __shared__ float4 sm4[];
+  Lay L{n, m, a.K};
   const size_t nsite = (size_t) n * n;
   const size_t per = (nsite + a.chunks - 1) / a.chunks;
   const size_t s0 = (size_t) chunk * per, s1 = s0 + per < nsite ? s0 + per : nsite;
-  for (size_t base = s0; base < s1; base += G2S) {
-    const int nts = (int) (s1 - base < (size_t) G2S ? s1 - base : (size_t) G2S);
-    __syncthreads();
-    // ---- staging ----
-    for (int w = tid; w < G2S * ns; w += G2T) {
-      int ts = w / ns, col = w % ns;
-      if (ts >= nts) continue;
-      size_t site = base + ts;
-      int i = (int) (site % n), j = (int) (site / n);
-      int b = col / m, v = col % m;
-      size_t o0 = L.edge(k, 0, 0, 0, v);
-      bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
-      cx<float>* fI = fi + ts * 3 * ns + col;
-      cx<float>* fJ = fj + ts * 3 * ns + col;
-      if (b == 0) {
-        // E column: float-float values, and their leading floats for the FP32 entries
-        const cdd* eb = (const cdd*) a.ptrs[0] + o0;
-        cx<dd>* dI = di + ts * 3 * m + v;
-        cx<dd>* dJ = dj + ts * 3 * m + v;
-        const dd kap = dd_make(a.kap.dd[2 * site], a.kap.dd[2 * site + 1]);
-        auto body = [&](const auto& E) {
-          cx<dd> x0 = E(0, i, j), t = E(0, i, j + 1);
-          dI[m] = x0;
-          fI[ns] = mkc(x0.re.hi, x0.im.hi);
-          cx<dd> mx = scal(sixth_d, scal(four_d, x0) + t + E(0, i, j - 1));
-          dJ[m] = mx;
-          fJ[ns] = mkc(mx.re.hi, mx.im.hi);
-          cx<dd> c = x0 - t;
-          cx<dd> y0 = E(1, i, j), r = E(1, i + 1, j);
-          dI[2 * m] = y0;
-          fI[2 * ns] = mkc(y0.re.hi, y0.im.hi);
-          cx<dd> my = scal(sixth_d, scal(four_d, y0) + r + E(1, i - 1, j));
-          dJ[2 * m] = my;
-          fJ[2 * ns] = mkc(my.re.hi, my.im.hi);
-          c = c - y0 + r;
-          dI[0] = c;
-          fI[0] = mkc(c.re.hi, c.im.hi);
-          cx<dd> kc = scal(kap, c);
-          dJ[0] = kc;
-          fJ[0] = mkc(kc.re.hi, kc.im.hi);
-        };
-        if (inner) body(EAI<cdd, dd>{eb, n, m});
-        else body(EA<cdd, dd>{eb, n, m, seam_load<dd>(a.ph, a.K, k, n)});
-      } else {
-        const float2* xb = (const float2*) a.ptrs[b] + o0;
-        const float kap = a.kap.f[site];
-        auto body = [&](const auto& X) {
-          cx<float> x0 = X(0, i, j), t = X(0, i, j + 1), y0 = X(1, i, j), r = X(1, i + 1, j);
-          cx<float> c = x0 - t - y0 + r;
-          fI[0] = c; fI[ns] = x0; fI[2 * ns] = y0;
-          fJ[0] = scal(kap, c);
-          fJ[ns] = scal(sixth_f, scal(4.0f, x0) + t + X(0, i, j - 1));
-          fJ[2 * ns] = scal(sixth_f, scal(4.0f, y0) + r + X(1, i - 1, j));
-        };
-        if (inner) body(EAI<float2, float>{xb, n, m});
-        else body(EA<float2, float>{xb, n, m, seam_load<float>(a.ph, a.K, k, n)});
-      }
-    }
-    if (use_r)
-      for (int w = tid; w < G2S * m; w += G2T) {
-        int ts = w / m, v = w % m;
-        if (ts >= nts) continue;
-        size_t site = base + ts;
-        int i = (int) (site % n), j = (int) (site / n);
-        float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
-        fr[ts * 2 * m + v] = mkc(rx.x, rx.y);
-        fr[ts * 2 * m + m + v] = mkc(ry.x, ry.y);
-      }
-    __syncthreads();
-    // ---- accumulation ----
-    if (ftile) {
-      for (int ts = 0; ts < nts; ts++) {
-        const cx<float>* I = fi + ts * 3 * ns;
-        const cx<float>* J = fj + ts * 3 * ns;
-        const cx<float>* Rr = fr + ts * 2 * m;
-        const cx<float> xr[2] = {I[ns + r0], I[ns + r1]}, yr[2] = {I[2 * ns + r0], I[2 * ns + r1]};
-        const cx<float> cr[2] = {I[r0], I[r1]};
+  const double axy = (double) n * (double) n;
+  double* out = a.partial + (((size_t) k * a.chunks + chunk) * nent) * 4;
+  const bool use_r = a.resid != nullptr;
+
+  if (role == 0) {
+    // ---------------- FP32 entries ----------------
+    // I[s][b-1][col][3]: curl, x, y of the c64 blocks b = 1, 2
+    // J[s][b][col][4]:  b = 0: M x, M y, r x, r y of E; b >= 1: kappa curl, M x, M y
+    cx<float>* I = reinterpret_cast<cx<float>*>(sm4);
+    cx<float>* J = I + GS_S * 2 * 16 * 3;
+    const int ntile = nb == 3 ? 136 : (nb == 2 ? 52 : 0);
+    const int tile = tid >> 1, g = tid & 1;
+    const bool live = tile < ntile;
+    int bi = 1, bj = 0, ti = 0, tj = 0;
+    if (live) gs_tile_f(tile, nb, bi, bj, ti, tj);
+    const bool rmode = use_r && bj == 0;
+    // rows/columns of the tile inside their blocks, clamped to m - 1 past the block
+    int rc_[4], cc_[2];
 #pragma unroll
-        for (int bq = 0; bq < 2; bq++) {
-          const int c = bq ? c1 : c0;
-          const cx<float> mx = J[ns + c], my = J[2 * ns + c];
-          cx<float> ka = mkc(0.f, 0.f), kb = mkc(0.f, 0.f);
-          if (rmode) {
-            ka = Rr[c];
-            kb = Rr[m + c];
-          } else {
-            ka = J[c];
+    for (int q = 0; q < 4; q++) rc_[q] = 4 * ti + q < m ? 4 * ti + q : m - 1;
+#pragma unroll
+    for (int q = 0; q < 2; q++) cc_[q] = 2 * tj + q < m ? 2 * tj + q : m - 1;
+    float acc[8][4];   // entry (2 aq + bq): A re, A im, M re, M im
+#pragma unroll
+    for (int e = 0; e < 8; e++) acc[e][0] = acc[e][1] = acc[e][2] = acc[e][3] = 0.f;
+    const float sixth = a.sixth.hi;
+    for (size_t base = s0; base < s1; base += GS_S) {
+      const int nts = (int) (s1 - base < (size_t) GS_S ? s1 - base : (size_t) GS_S);
+      __syncthreads();
+      for (int w = tid; w < GS_S * nb * m; w += GS_T) {
+        const int ts = w / (nb * m), col = w % (nb * m);
+        if (ts >= nts) continue;
+        const size_t site = base + ts;
+        const int i = (int) (site % n), j = (int) (site / n);
+        const int b = col / m, v = col % m;
+        const size_t o0 = L.edge(k, 0, 0, 0, v);
+        const bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
+        cx<float>* Jp = J + ((size_t) (ts * 3 + b) * 16 + v) * 4;
+        if (b == 0) {
+          const cdd* eb = (const cdd*) a.ptrs[0] + o0;
+          auto body = [&](const auto& E) {
+            const cx<float> x0 = E(0, i, j), y0 = E(1, i, j);
+            Jp[0] = scal(sixth, scal(4.0f, x0) + E(0, i, j + 1) + E(0, i, j - 1));
+            Jp[1] = scal(sixth, scal(4.0f, y0) + E(1, i + 1, j) + E(1, i - 1, j));
+          };
+          if (inner) body(EAI<cdd, float>{eb, n, m});
+          else body(EA<cdd, float>{eb, n, m, seam_load<float>(a.ph, a.K, k, n)});
+          if (use_r) {
+            const float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
+            Jp[2] = mkc(rx.x, rx.y);
+            Jp[3] = mkc(ry.x, ry.y);
+          }
+        } else {
+          const float2* xb = (const float2*) a.ptrs[b] + o0;
+          const float kap = a.kap.f[site];
+          cx<float>* Ip = I + ((size_t) (ts * 2 + b - 1) * 16 + v) * 3;
+          auto body = [&](const auto& X) {
+            const cx<float> x0 = X(0, i, j), t = X(0, i, j + 1), y0 = X(1, i, j), r = X(1, i + 1, j);
+            const cx<float> c = x0 - t - y0 + r;
+            Ip[0] = c; Ip[1] = x0; Ip[2] = y0;
+            Jp[0] = scal(kap, c);
+            Jp[1] = scal(sixth, scal(4.0f, x0) + t + X(0, i, j - 1));
+            Jp[2] = scal(sixth, scal(4.0f, y0) + r + X(1, i - 1, j));
+          };
+          if (inner) body(EAI<float2, float>{xb, n, m});
+          else body(EA<float2, float>{xb, n, m, seam_load<float>(a.ph, a.K, k, n)});
+        }
+      }
+      __syncthreads();
+      if (live) {
+        for (int ts = g; ts < nts; ts += 2) {
+          const cx<float>* Ib = I + (size_t) (ts * 2 + bi - 1) * 16 * 3;
+          const cx<float>* Jb = J + (size_t) (ts * 3 + bj) * 16 * 4;
+          cx<float> cr[4], xr[4], yr[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            cr[q] = Ib[rc_[q] * 3 + 0];
+            xr[q] = Ib[rc_[q] * 3 + 1];
+            yr[q] = Ib[rc_[q] * 3 + 2];
           }
 #pragma unroll
-          for (int aq = 0; aq < 2; aq++) {
-            float* d = acc + 4 * (2 * aq + bq);
-            // M: conj(x) Mx + conj(y) My
-            d[2] = fmaf(xr[aq].re, mx.re, d[2]); d[2] = fmaf(xr[aq].im, mx.im, d[2]);
-            d[2] = fmaf(yr[aq].re, my.re, d[2]); d[2] = fmaf(yr[aq].im, my.im, d[2]);
-            d[3] = fmaf(xr[aq].re, mx.im, d[3]); d[3] = fmaf(-xr[aq].im, mx.re, d[3]);
-            d[3] = fmaf(yr[aq].re, my.im, d[3]); d[3] = fmaf(-yr[aq].im, my.re, d[3]);
+          for (int bq = 0; bq < 2; bq++) {
+            const cx<float>* Jc = Jb + cc_[bq] * 4;
             if (rmode) {
-              // A as s^H r: conj(x) rx + conj(y) ry
-              d[0] = fmaf(xr[aq].re, ka.re, d[0]); d[0] = fmaf(xr[aq].im, ka.im, d[0]);
-              d[0] = fmaf(yr[aq].re, kb.re, d[0]); d[0] = fmaf(yr[aq].im, kb.im, d[0]);
-              d[1] = fmaf(xr[aq].re, ka.im, d[1]); d[1] = fmaf(-xr[aq].im, ka.re, d[1]);
-              d[1] = fmaf(yr[aq].re, kb.im, d[1]); d[1] = fmaf(-yr[aq].im, kb.re, d[1]);
+              const cx<float> mx = Jc[0], my = Jc[1], rx = Jc[2], ry = Jc[3];
+#pragma unroll
+              for (int aq = 0; aq < 4; aq++) {
+                float* d = acc[2 * aq + bq];
+                d[2] = fmaf(xr[aq].re, mx.re, d[2]); d[2] = fmaf(xr[aq].im, mx.im, d[2]);
+                d[2] = fmaf(yr[aq].re, my.re, d[2]); d[2] = fmaf(yr[aq].im, my.im, d[2]);
+                d[3] = fmaf(xr[aq].re, mx.im, d[3]); d[3] = fmaf(-xr[aq].im, mx.re, d[3]);
+                d[3] = fmaf(yr[aq].re, my.im, d[3]); d[3] = fmaf(-yr[aq].im, my.re, d[3]);
+                d[0] = fmaf(xr[aq].re, rx.re, d[0]); d[0] = fmaf(xr[aq].im, rx.im, d[0]);
+                d[0] = fmaf(yr[aq].re, ry.re, d[0]); d[0] = fmaf(yr[aq].im, ry.im, d[0]);
+                d[1] = fmaf(xr[aq].re, rx.im, d[1]); d[1] = fmaf(-xr[aq].im, rx.re, d[1]);
+                d[1] = fmaf(yr[aq].re, ry.im, d[1]); d[1] = fmaf(-yr[aq].im, ry.re, d[1]);
+              }
             } else {
-              // A: conj(curl) kappa curl
-              d[0] = fmaf(cr[aq].re, ka.re, d[0]); d[0] = fmaf(cr[aq].im, ka.im, d[0]);
-              d[1] = fmaf(cr[aq].re, ka.im, d[1]); d[1] = fmaf(-cr[aq].im, ka.re, d[1]);
+              const cx<float> kc = Jc[0], mx = Jc[1], my = Jc[2];
+#pragma unroll
+              for (int aq = 0; aq < 4; aq++) {
+                float* d = acc[2 * aq + bq];
+                d[2] = fmaf(xr[aq].re, mx.re, d[2]); d[2] = fmaf(xr[aq].im, mx.im, d[2]);
+                d[2] = fmaf(yr[aq].re, my.re, d[2]); d[2] = fmaf(yr[aq].im, my.im, d[2]);
+                d[3] = fmaf(xr[aq].re, mx.im, d[3]); d[3] = fmaf(-xr[aq].im, mx.re, d[3]);
+                d[3] = fmaf(yr[aq].re, my.im, d[3]); d[3] = fmaf(-yr[aq].im, my.re, d[3]);
+                d[0] = fmaf(cr[aq].re, kc.re, d[0]); d[0] = fmaf(cr[aq].im, kc.im, d[0]);
+                d[1] = fmaf(cr[aq].re, kc.im, d[1]); d[1] = fmaf(-cr[aq].im, kc.re, d[1]);
+              }
             }
           }
         }
       }
-    } else if (drole) {
-      for (int ts = half; ts < nts; ts += 2) {
-        const cx<dd>* I = di + ts * 3 * m;
-        const cx<dd>* J = dj + ts * 3 * m;
-        comp_cmac(eacc_a, I[ei], J[ej]);
-        comp_cmac(eacc_m, I[m + ei], J[m + ej]);
-        comp_cmac(eacc_m, I[2 * m + ei], J[2 * m + ej]);
+    }
+    // the two threads of a tile meet; the first writes the tile's entries,
+    // A from its parts: s^H r + theta s^H M e (residual form) or axy curl + M
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      double q[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        q[c] = (double) acc[e][c];
+        q[c] += __shfl_xor_sync(0xffffffffu, q[c], 1);
+      }
+      const int rl = 4 * ti + (e >> 1), cl = 2 * tj + (e & 1);
+      if (g == 0 && live && rl < m && cl < m && !(bi == bj && rl < cl)) {
+        const int r = bi * m + rl, col = bj * m + cl;
+        double* o = out + (size_t) (r * (r + 1) / 2 + col) * 4;
+        if (rmode) {
+          const double th = a.theta[(size_t) k * m + cl];
+          o[0] = th * q[2] + q[0];
+          o[1] = th * q[3] + q[1];
+        } else {
+          o[0] = axy * q[0] + q[2];
+          o[1] = axy * q[1] + q[3];
+        }
+        o[2] = q[2];
+        o[3] = q[3];
       }
     }
-  }
-  // ---- partial sums of this CTA ----
-  __syncthreads();
-  double axy = (double) n * (double) n;
-  double* out = a.partial + (((size_t) k * a.chunks + chunk) * nent) * 4;
-  auto put = [&](int i, int j, double ar, double ai, double mr, double mi) {
-    int e = i * (i + 1) / 2 + j;
-    if (use_r && i >= m && j < m) {
-      double th = a.theta[(size_t) k * m + j];
-      out[(size_t) e * 4 + 0] = th * mr + ar;
-      out[(size_t) e * 4 + 1] = th * mi + ai;
-    } else {
-      out[(size_t) e * 4 + 0] = axy * ar + mr;
-      out[(size_t) e * 4 + 1] = axy * ai + mi;
-    }
-    out[(size_t) e * 4 + 2] = mr;
-    out[(size_t) e * 4 + 3] = mi;
-  };
-  if (ftile)
+  } else {
+    // ---------------- E-E entries ----------------
+    // DI[s][col][3]: curl, x, y;  DJ[s][col][3]: kappa curl, M x, M y (float-float)
+    cx<dd>* DI = reinterpret_cast<cx<dd>*>(sm4);
+    cx<dd>* DJ = DI + GS_S * 16 * 3;
+    const int tile = tid >> 3, g = tid & 7;
+    const bool live = tile < 36;
+    int ti = 0, tj = 0;
+    if (live) tri_index(tile, ti, tj);
+    const int r0 = 2 * ti < m ? 2 * ti : m - 1, r1 = 2 * ti + 1 < m ? 2 * ti + 1 : m - 1;
+    const int c0 = 2 * tj < m ? 2 * tj : m - 1, c1 = 2 * tj + 1 < m ? 2 * tj + 1 : m - 1;
+    float ea[4][4], em[4][4];   // entry (2a + b): re s, re c, im s, im c
 #pragma unroll
-    for (int aq = 0; aq < 2; aq++)
+    for (int e = 0; e < 4; e++)
 #pragma unroll
-      for (int bq = 0; bq < 2; bq++) {
-        const int r = aq ? r1 : r0, c = bq ? c1 : c0;
-        // skip the repeated row or column and the upper entry of a diagonal tile
-        if ((aq && r1 == r0) || (bq && c1 == c0) || (tbi == tbj && r - tbi * m < c - tbj * m)) continue;
-        const float* d = acc + 4 * (2 * aq + bq);
-        put(r, c, d[0], d[1], d[2], d[3]);
+      for (int c = 0; c < 4; c++) ea[e][c] = em[e][c] = 0.f;
+    const dd sixth_d = sget<dd>(a.sixth), four_d = rc<dd>(4.0f);
+    for (size_t base = s0; base < s1; base += GS_S) {
+      const int nts = (int) (s1 - base < (size_t) GS_S ? s1 - base : (size_t) GS_S);
+      __syncthreads();
+      for (int w = tid; w < GS_S * m; w += GS_T) {
+        const int ts = w / m, v = w % m;
+        if (ts >= nts) continue;
+        const size_t site = base + ts;
+        const int i = (int) (site % n), j = (int) (site / n);
+        const size_t o0 = L.edge(k, 0, 0, 0, v);
+        const bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
+        const cdd* eb = (const cdd*) a.ptrs[0] + o0;
+        const dd kap = dd_make(a.kap.dd[2 * site], a.kap.dd[2 * site + 1]);
+        cx<dd>* Ip = DI + ((size_t) ts * 16 + v) * 3;
+        cx<dd>* Jp = DJ + ((size_t) ts * 16 + v) * 3;
+        auto body = [&](const auto& E) {
+          const cx<dd> x0 = E(0, i, j), t = E(0, i, j + 1), y0 = E(1, i, j), r = E(1, i + 1, j);
+          const cx<dd> c = x0 - t - y0 + r;
+          Ip[0] = c; Ip[1] = x0; Ip[2] = y0;
+          Jp[0] = scal(kap, c);
+          Jp[1] = scal(sixth_d, scal(four_d, x0) + t + E(0, i, j - 1));
+          Jp[2] = scal(sixth_d, scal(four_d, y0) + r + E(1, i - 1, j));
+        };
+        if (inner) body(EAI<cdd, dd>{eb, n, m});
+        else body(EA<cdd, dd>{eb, n, m, seam_load<dd>(a.ph, a.K, k, n)});
       }
-  // the two halves of every E-E entry meet in shared memory
-  double* xch = reinterpret_cast<double*>(sm2);     // [ment][4]
-  if (drole && half == 1) {
-    double* q = xch + (size_t) (u >> 1) * 4;
-    q[0] = (double) eacc_a[0] + (double) eacc_a[1];
-    q[1] = (double) eacc_a[2] + (double) eacc_a[3];
-    q[2] = (double) eacc_m[0] + (double) eacc_m[1];
-    q[3] = (double) eacc_m[2] + (double) eacc_m[3];
-  }
-  __syncthreads();
-  if (drole && half == 0) {
-    const double* q = xch + (size_t) (u >> 1) * 4;
-    put(ei, ej, (double) eacc_a[0] + (double) eacc_a[1] + q[0], (double) eacc_a[2] + (double) eacc_a[3] + q[1],
-        (double) eacc_m[0] + (double) eacc_m[1] + q[2], (double) eacc_m[2] + (double) eacc_m[3] + q[3]);
+      __syncthreads();
+      if (live) {
+        for (int ts = g; ts < nts; ts += 8) {
+          const cx<dd>* Is = DI + (size_t) ts * 16 * 3;
+          const cx<dd>* Js = DJ + (size_t) ts * 16 * 3;
+          const cx<dd> Ir[2][3] = {{Is[r0 * 3], Is[r0 * 3 + 1], Is[r0 * 3 + 2]},
+                                   {Is[r1 * 3], Is[r1 * 3 + 1], Is[r1 * 3 + 2]}};
+#pragma unroll
+          for (int bq = 0; bq < 2; bq++) {
+            const int cq = bq ? c1 : c0;
+            const cx<dd> kc = Js[cq * 3], mx = Js[cq * 3 + 1], my = Js[cq * 3 + 2];
+#pragma unroll
+            for (int aq = 0; aq < 2; aq++) {
+              comp_cmac(ea[2 * aq + bq], Ir[aq][0], kc);
+              comp_cmac(em[2 * aq + bq], Ir[aq][1], mx);
+              comp_cmac(em[2 * aq + bq], Ir[aq][2], my);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      double q[4] = {(double) ea[e][0] + (double) ea[e][1], (double) ea[e][2] + (double) ea[e][3],
+                     (double) em[e][0] + (double) em[e][1], (double) em[e][2] + (double) em[e][3]};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        q[c] += __shfl_xor_sync(0xffffffffu, q[c], 1);
+        q[c] += __shfl_xor_sync(0xffffffffu, q[c], 2);
+        q[c] += __shfl_xor_sync(0xffffffffu, q[c], 4);
+      }
+      const int aq = e >> 1, bq = e & 1;
+      const int rl = 2 * ti + aq, cl = 2 * tj + bq;
+      if (g == 0 && live && rl < m && cl < m && rl >= cl) {
+        double* o = out + (size_t) (rl * (rl + 1) / 2 + cl) * 4;
+        o[0] = axy * q[0] + q[2];
+        o[1] = axy * q[1] + q[3];
+        o[2] = q[2];
+        o[3] = q[3];
+      }
+    }
   }
 }
 
-static size_t gram_mixed_smem(int ns, int m) {
-  return sizeof(cx<float>) * G2S * (6 * ns + 2 * m) + sizeof(cx<dd>) * G2S * 6 * m;
+static size_t gram_split_smem() {
+  const size_t f = sizeof(cx<float>) * GS_S * (2 * 16 * 3 + 3 * 16 * 4);
+  const size_t d = sizeof(cx<dd>) * GS_S * 16 * 3 * 2;
+  return f > d ? f : d;
 }
+
 
 static int gram_chunks(int K, size_t nsite) {
   int c = (g_tuning.gram_waves * sm_count() + K - 1) / K;
@@ -1024,9 +1063,9 @@ extern "C" int mxk_block_gram(int n, int m, int K, const double* ph, mxk_kappa k
   bool lo_rest = true;
   for (int q = 1; q < nb; q++) lo_rest = lo_rest && precs[q] == MX_C64;
   if (hi_dd && lo_rest && m <= 16 && nb <= 3 && (nb == 1 || resid)) {
-    size_t sm = gram_mixed_smem(a.ns, m);
-    cudaFuncSetAttribute(k_block_gram_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
-    k_block_gram_mixed<<<g, G2T, sm, st>>>(a);
+    size_t sm = gram_split_smem();
+    cudaFuncSetAttribute(k_block_gram_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    k_block_gram_split<<<dim3(a.chunks, K, nb > 1 ? 2 : 1), GS_T, sm, st>>>(a);
   } else if (hi_dd) {
     cudaFuncSetAttribute(k_block_gram<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     for (int eb = 0; eb < nent; eb += 5 * GT) k_block_gram<dd><<<g, GT, smem, st>>>(a, mh, eb);
