@@ -776,8 +776,9 @@ __device__ __forceinline__ void gs_tile_f(int q, int nb, int& bi, int& bj, int& 
 }
 
 __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
-  const int k = blockIdx.y, chunk = blockIdx.x, role = blockIdx.z;
   const int n = a.n, m = a.m, ns = a.ns, nb = a.nb;
+  // a single block has E-E entries only (grid z = 1)
+  const int k = blockIdx.y, chunk = blockIdx.x, role = nb > 1 ? (int) blockIdx.z : 1;
   const int nent = ns * (ns + 1) / 2;
   const int tid = threadIdx.x;
   extern __shared__ float4 sm4[];
