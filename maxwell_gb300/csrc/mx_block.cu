@@ -755,6 +755,13 @@ __device__ __forceinline__ void tri_index(int e, int& i, int& j) {
 // ------------------------------------------------------------------
 constexpr int GS_T = 288;   // threads per CTA
 constexpr int GS_S = 32;    // sites per tile
+// shared layouts, component-major within a site and a site stride one
+// element past a multiple of 32 banks, so that the threads of a warp (tiles
+// x neighbouring sites) hit distinct banks:
+//   FP32 I (ts, b-1, comp, col) = ts * GS_IS + ((b - 1) * 3 + comp) * 16 + col
+//   FP32 J (ts, b, comp, col)   = ts * GS_JS + (b * 4 + comp) * 16 + col
+//   E-E  D (ts, comp, col)      = ts * GS_DS + comp * 16 + col
+constexpr int GS_IS = 2 * 3 * 16 + 1, GS_JS = 3 * 4 * 16 + 1, GS_DS = 3 * 16 + 1;
 
 // FP32 tiles are 4 rows x 2 columns: 32 per full block pair (1,0), (2,0),
 // (2,1) with bi < nb, then 20 per diagonal block (1,1), (2,2) (the tiles with
@@ -795,7 +802,7 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
     // I[s][b-1][col][3]: curl, x, y of the c64 blocks b = 1, 2
     // J[s][b][col][4]:  b = 0: M x, M y, r x, r y of E; b >= 1: kappa curl, M x, M y
     cx<float>* I = reinterpret_cast<cx<float>*>(sm4);
-    cx<float>* J = I + GS_S * 2 * 16 * 3;
+    cx<float>* J = I + GS_S * GS_IS;
     const int ntile = nb == 3 ? 136 : (nb == 2 ? 52 : 0);
     const int tile = tid >> 1, g = tid & 1;
     const bool live = tile < ntile;
@@ -823,32 +830,32 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
         const int b = col / m, v = col % m;
         const size_t o0 = L.edge(k, 0, 0, 0, v);
         const bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
-        cx<float>* Jp = J + ((size_t) (ts * 3 + b) * 16 + v) * 4;
+        cx<float>* Jp = J + (size_t) ts * GS_JS + b * 64 + v;   // component c at Jp[16 c]
         if (b == 0) {
           const cdd* eb = (const cdd*) a.ptrs[0] + o0;
           auto body = [&](const auto& E) {
             const cx<float> x0 = E(0, i, j), y0 = E(1, i, j);
             Jp[0] = scal(sixth, scal(4.0f, x0) + E(0, i, j + 1) + E(0, i, j - 1));
-            Jp[1] = scal(sixth, scal(4.0f, y0) + E(1, i + 1, j) + E(1, i - 1, j));
+            Jp[16] = scal(sixth, scal(4.0f, y0) + E(1, i + 1, j) + E(1, i - 1, j));
           };
           if (inner) body(EAI<cdd, float>{eb, n, m});
           else body(EA<cdd, float>{eb, n, m, seam_load<float>(a.ph, a.K, k, n)});
           if (use_r) {
             const float2 rx = a.resid[L.edge(k, 0, j, i, v)], ry = a.resid[L.edge(k, 1, j, i, v)];
-            Jp[2] = mkc(rx.x, rx.y);
-            Jp[3] = mkc(ry.x, ry.y);
+            Jp[32] = mkc(rx.x, rx.y);
+            Jp[48] = mkc(ry.x, ry.y);
           }
         } else {
           const float2* xb = (const float2*) a.ptrs[b] + o0;
           const float kap = a.kap.f[site];
-          cx<float>* Ip = I + ((size_t) (ts * 2 + b - 1) * 16 + v) * 3;
+          cx<float>* Ip = I + (size_t) ts * GS_IS + (b - 1) * 48 + v;   // component c at Ip[16 c]
           auto body = [&](const auto& X) {
             const cx<float> x0 = X(0, i, j), t = X(0, i, j + 1), y0 = X(1, i, j), r = X(1, i + 1, j);
             const cx<float> c = x0 - t - y0 + r;
-            Ip[0] = c; Ip[1] = x0; Ip[2] = y0;
+            Ip[0] = c; Ip[16] = x0; Ip[32] = y0;
             Jp[0] = scal(kap, c);
-            Jp[1] = scal(sixth, scal(4.0f, x0) + t + X(0, i, j - 1));
-            Jp[2] = scal(sixth, scal(4.0f, y0) + r + X(1, i - 1, j));
+            Jp[16] = scal(sixth, scal(4.0f, x0) + t + X(0, i, j - 1));
+            Jp[32] = scal(sixth, scal(4.0f, y0) + r + X(1, i - 1, j));
           };
           if (inner) body(EAI<float2, float>{xb, n, m});
           else body(EA<float2, float>{xb, n, m, seam_load<float>(a.ph, a.K, k, n)});
@@ -857,20 +864,20 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
       __syncthreads();
       if (live) {
         for (int ts = g; ts < nts; ts += 2) {
-          const cx<float>* Ib = I + (size_t) (ts * 2 + bi - 1) * 16 * 3;
-          const cx<float>* Jb = J + (size_t) (ts * 3 + bj) * 16 * 4;
+          const cx<float>* Ib = I + (size_t) ts * GS_IS + (bi - 1) * 48;
+          const cx<float>* Jb = J + (size_t) ts * GS_JS + bj * 64;
           cx<float> cr[4], xr[4], yr[4];
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            cr[q] = Ib[rc_[q] * 3 + 0];
-            xr[q] = Ib[rc_[q] * 3 + 1];
-            yr[q] = Ib[rc_[q] * 3 + 2];
+            cr[q] = Ib[rc_[q]];
+            xr[q] = Ib[16 + rc_[q]];
+            yr[q] = Ib[32 + rc_[q]];
           }
 #pragma unroll
           for (int bq = 0; bq < 2; bq++) {
-            const cx<float>* Jc = Jb + cc_[bq] * 4;
+            const cx<float>* Jc = Jb + cc_[bq];
             if (rmode) {
-              const cx<float> mx = Jc[0], my = Jc[1], rx = Jc[2], ry = Jc[3];
+              const cx<float> mx = Jc[0], my = Jc[16], rx = Jc[32], ry = Jc[48];
 #pragma unroll
               for (int aq = 0; aq < 4; aq++) {
                 float* d = acc[2 * aq + bq];
@@ -884,7 +891,7 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
                 d[1] = fmaf(yr[aq].re, ry.im, d[1]); d[1] = fmaf(-yr[aq].im, ry.re, d[1]);
               }
             } else {
-              const cx<float> kc = Jc[0], mx = Jc[1], my = Jc[2];
+              const cx<float> kc = Jc[0], mx = Jc[16], my = Jc[32];
 #pragma unroll
               for (int aq = 0; aq < 4; aq++) {
                 float* d = acc[2 * aq + bq];
@@ -930,7 +937,7 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
     // ---------------- E-E entries ----------------
     // DI[s][col][3]: curl, x, y;  DJ[s][col][3]: kappa curl, M x, M y (float-float)
     cx<dd>* DI = reinterpret_cast<cx<dd>*>(sm4);
-    cx<dd>* DJ = DI + GS_S * 16 * 3;
+    cx<dd>* DJ = DI + GS_S * GS_DS;
     const int tile = tid >> 3, g = tid & 7;
     const bool live = tile < 36;
     int ti = 0, tj = 0;
@@ -955,15 +962,15 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
         const bool inner = i > 0 && i < n - 1 && j > 0 && j < n - 1;
         const cdd* eb = (const cdd*) a.ptrs[0] + o0;
         const dd kap = dd_make(a.kap.dd[2 * site], a.kap.dd[2 * site + 1]);
-        cx<dd>* Ip = DI + ((size_t) ts * 16 + v) * 3;
-        cx<dd>* Jp = DJ + ((size_t) ts * 16 + v) * 3;
+        cx<dd>* Ip = DI + (size_t) ts * GS_DS + v;   // component c at Ip[16 c]
+        cx<dd>* Jp = DJ + (size_t) ts * GS_DS + v;
         auto body = [&](const auto& E) {
           const cx<dd> x0 = E(0, i, j), t = E(0, i, j + 1), y0 = E(1, i, j), r = E(1, i + 1, j);
           const cx<dd> c = x0 - t - y0 + r;
-          Ip[0] = c; Ip[1] = x0; Ip[2] = y0;
+          Ip[0] = c; Ip[16] = x0; Ip[32] = y0;
           Jp[0] = scal(kap, c);
-          Jp[1] = scal(sixth_d, scal(four_d, x0) + t + E(0, i, j - 1));
-          Jp[2] = scal(sixth_d, scal(four_d, y0) + r + E(1, i - 1, j));
+          Jp[16] = scal(sixth_d, scal(four_d, x0) + t + E(0, i, j - 1));
+          Jp[32] = scal(sixth_d, scal(four_d, y0) + r + E(1, i - 1, j));
         };
         if (inner) body(EAI<cdd, dd>{eb, n, m});
         else body(EA<cdd, dd>{eb, n, m, seam_load<dd>(a.ph, a.K, k, n)});
@@ -971,14 +978,13 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
       __syncthreads();
       if (live) {
         for (int ts = g; ts < nts; ts += 8) {
-          const cx<dd>* Is = DI + (size_t) ts * 16 * 3;
-          const cx<dd>* Js = DJ + (size_t) ts * 16 * 3;
-          const cx<dd> Ir[2][3] = {{Is[r0 * 3], Is[r0 * 3 + 1], Is[r0 * 3 + 2]},
-                                   {Is[r1 * 3], Is[r1 * 3 + 1], Is[r1 * 3 + 2]}};
+          const cx<dd>* Is = DI + (size_t) ts * GS_DS;
+          const cx<dd>* Js = DJ + (size_t) ts * GS_DS;
+          const cx<dd> Ir[2][3] = {{Is[r0], Is[16 + r0], Is[32 + r0]}, {Is[r1], Is[16 + r1], Is[32 + r1]}};
 #pragma unroll
           for (int bq = 0; bq < 2; bq++) {
             const int cq = bq ? c1 : c0;
-            const cx<dd> kc = Js[cq * 3], mx = Js[cq * 3 + 1], my = Js[cq * 3 + 2];
+            const cx<dd> kc = Js[cq], mx = Js[16 + cq], my = Js[32 + cq];
 #pragma unroll
             for (int aq = 0; aq < 2; aq++) {
               comp_cmac(ea[2 * aq + bq], Ir[aq][0], kc);
@@ -1013,8 +1019,8 @@ __global__ void __launch_bounds__(GS_T, 2) k_block_gram_split(GramArgs a) {
 }
 
 static size_t gram_split_smem() {
-  const size_t f = sizeof(cx<float>) * GS_S * (2 * 16 * 3 + 3 * 16 * 4);
-  const size_t d = sizeof(cx<dd>) * GS_S * 16 * 3 * 2;
+  const size_t f = sizeof(cx<float>) * GS_S * (GS_IS + GS_JS);
+  const size_t d = sizeof(cx<dd>) * GS_S * GS_DS * 2;
   return f > d ? f : d;
 }
 

@@ -570,30 +570,6 @@ __global__ void k_edge_gs_rowpair(int n, int m, int K, const double* __restrict_
     afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, (F + n - 1) % n, j, k, v, b, x);
 }
 
-// Two vertex rows j and j+2 of one parity per CTA, walking the same chunks
-// side by side: the x row j+1 between them is read by both within a few
-// hundred cycles, so the second read hits L1 and a launch reads about 1.25
-// instead of 1.5 x blocks.  Patch order as k_edge_gs_rowpair.
-template <typename S, typename R>
-__global__ void __launch_bounds__(512) k_edge_gs_rowpair2(int n, int m, int K, const double* __restrict__ ph, Kap<R> kap,
-                                   const float4* __restrict__ ftab, Sc axy_s, Sc mm_s, Sc s8_s, Sc is8_s, int cj,
-                                   int rev, const S* __restrict__ b, S* x) {
-  // block (m, 2P): x = vector, y = row half x patch lane; grid (row pairs of the parity, K)
-  const int k = blockIdx.y, v = threadIdx.x, P = blockDim.y / 2, h = n / 2;
-  const int half = threadIdx.y / P, lane = threadIdx.y - half * P;
-  const int j = 2 * (2 * blockIdx.x + half) + cj, F = rev;
-  for (int c = 0; c < h; c += P) {
-    const int p = c + lane;
-    if (p < h) afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, 2 * p + F, j, k, v, b, x);
-    __syncthreads();
-    if (p < h && p >= 1)
-      afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, 2 * p + F - 1, j, k, v, b, x);
-    __syncthreads();
-  }
-  if (lane == 0)
-    afw_patch<S, R>(n, m, K, ph, kap, ftab, axy_s, mm_s, s8_s, is8_s, (F + n - 1) % n, j, k, v, b, x);
-}
-
 // ------------------------------------------------------------------
 // edge transfers (gather form of prolongation_edge2d / restriction_edge2d)
 // ------------------------------------------------------------------
@@ -1412,14 +1388,9 @@ static int L_edge_gs_rowpair(int n, int m, int K, const double* ph, mxk_kappa ka
                              int cj, int rev, const void* b, void* x, cudaStream_t st) {
   const float4* ftab = (sizeof(R) == 4 && kap.afw && kap.afw_alpha == alpha && kap.afw_beta == beta)
                            ? (const float4*) kap.afw : nullptr;
-  if ((n / 2) % 2 == 0 && 512 % m == 0)
-    k_edge_gs_rowpair2<S, R><<<dim3(n / 4, K), dim3(m, 512 / m), 0, st>>>(
-        n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
-        make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), cj, rev, (const S*) b, (S*) x);
-  else
-    k_edge_gs_rowpair<S, R><<<dim3(n / 2, K), blk2(m), 0, st>>>(
-        n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
-        make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), cj, rev, (const S*) b, (S*) x);
+  k_edge_gs_rowpair<S, R><<<dim3(n / 2, K), blk2(m), 0, st>>>(
+      n, m, K, ph, make_kap<R>(kap, n), ftab, make_sc(alpha * (double) n * (double) n), make_sc(beta / 6.0),
+      make_sc(8.0 * beta / 6.0), make_sc(6.0 / (8.0 * beta)), cj, rev, (const S*) b, (S*) x);
   MX_CHECK_LAUNCH();
   return 0;
 }
