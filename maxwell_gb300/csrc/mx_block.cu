@@ -560,9 +560,14 @@ __global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void*
   const int k = blockIdx.y, m = a.m, nb = a.nb, nsrc = nb * m;
   extern __shared__ float4 smct[];
   float4* cS = smct;                                             // [48][16] coefficient pairs [row][column]
-  float4* tE = cS + 48 * 16;                                     // [2][CTE * 16] float-float source tiles
-  float2* tF = reinterpret_cast<float2*>(tE + 2 * CTE * 16);     // [2][2][CTE * 16] c64 source tiles
+  float4* tE = cS + 48 * 16;                                     // [2][CTE * 17] float-float source tiles
+  float2* tF = reinterpret_cast<float2*>(tE + 2 * CTE * 17);     // [2][2][CTE * 18] c64 source tiles
   const int tid = threadIdx.x;
+  // entry strides of the tiles: one float4 / one 16-byte unit past m, so
+  // that the four entries a warp reads at once fall on distinct banks (an
+  // odd m keeps the c64 tile unpadded: its 16-byte copies would straddle
+  // entries)
+  const int SE = m + 1, SF = (m & 1) ? m : m + 2;
   for (int q = tid; q < nsrc * m; q += CT) {
     int i = q / m, j = q % m;
     cS[i * 16 + j] = a.cpair[(size_t) k * a.ldc * m + (size_t) j * a.ldc + a.row0 + i];
@@ -582,12 +587,18 @@ __global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void*
     for (int b = 0; b < nb; b++) {
       if (b == 0 && dd0) {
         const float4* src = (const float4*) a.ptrs[0] + off;
-        float4* dst = tE + q * CTE * 16;
-        for (int u = tid; u < len; u += CT) cp_async16(dst + u, src + u);
+        float4* dst = tE + q * CTE * 17;
+        for (int u = tid; u < len; u += CT) {
+          const int e = u / m;
+          cp_async16(dst + e * SE + (u - e * m), src + u);
+        }
       } else {
         const float2* src = (const float2*) a.ptrs[b] + off;
-        float2* dst = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 16;
-        for (int u = 2 * tid; u < len; u += 2 * CT) cp_async16(dst + u, src + u);
+        float2* dst = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 18;
+        for (int u = 2 * tid; u < len; u += 2 * CT) {
+          const int e = u / m;
+          cp_async16(dst + e * SF + (u - e * m), src + u);
+        }
       }
     }
   };
@@ -609,11 +620,11 @@ __global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void*
       float fre[4] = {}, fim[4] = {};
       int row = 0;
       if (dd0) {
-        const float4* tEq = tE + q * CTE * 16;
+        const float4* tEq = tE + q * CTE * 17;
 #pragma unroll 4
         for (int i = 0; i < m; i++) {
           const float4 c[2] = {cS[i * 16 + c0], cS[i * 16 + c1]};
-          const float4 v[2] = {tEq[ea * m + i], tEq[eb * m + i]};
+          const float4 v[2] = {tEq[ea * SE + i], tEq[eb * SE + i]};
 #pragma unroll
           for (int r = 0; r < 2; r++)
 #pragma unroll
@@ -628,11 +639,11 @@ __global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void*
         row = m;
       }
       for (int b = dd0 ? 1 : 0; b < nb; b++) {
-        const float2* tb = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 16;
+        const float2* tb = tF + (q * 2 + (dd0 ? b - 1 : b)) * CTE * 18;
 #pragma unroll 4
         for (int i = 0; i < m; i++) {
           const float4 c[2] = {cS[(row + i) * 16 + c0], cS[(row + i) * 16 + c1]};
-          const float2 v[2] = {tb[ea * m + i], tb[eb * m + i]};
+          const float2 v[2] = {tb[ea * SF + i], tb[eb * SF + i]};
 #pragma unroll
           for (int r = 0; r < 2; r++)
 #pragma unroll
@@ -665,7 +676,7 @@ __global__ void __launch_bounds__(CT, 2) k_block_combine_tiled(CombArgs a, void*
 }
 
 static size_t combine_tiled_smem() {
-  return sizeof(float4) * (48 * 16 + 2 * CTE * 16) + sizeof(float2) * 4 * CTE * 16;
+  return sizeof(float4) * (48 * 16 + 2 * CTE * 17) + sizeof(float2) * 4 * CTE * 18;
 }
 
 // ------------------------------------------------------------------
