@@ -226,8 +226,8 @@ def fp64_residual_check(mx, n, kap, fac, lam, vec) -> float:
 # full 32-k workload holds > 30 GB on the device): node GS sweep
 # (profiles/node_gs_512x512_k4_ncu.md), AFW sweep
 # (profiles/afw_rowpair_512x512_k4_ncu.md), Gram
-# (profiles/block_gram_mixed_512x512_k4_ncu.md)
-TRAFFIC_32K = {"node_gs": 8 * 484.0e6, "afw": 8 * 2 * 648.1e6, "gram": 8 * 2.514e9}
+# (profiles/block_gram_split_512x512_k4_ncu.md)
+TRAFFIC_32K = {"node_gs": 8 * 484.0e6, "afw": 8 * 2 * 648.1e6, "gram": 8 * 3.501e9}
 
 
 def run_ours(args):
