@@ -287,6 +287,9 @@ typedef struct {
   int refine;            /* 1: after the finest level converges, one more block step with
                           * every search column in the Ritz basis (the refinement sweep
                           * of the 2048^2 configuration), residuals recomputed after it */
+  double nested_tol;     /* stopping tolerance of the nested iteration's coarser levels
+                          * (the reference's 'r' rule stops them at a defect of 1e-2,
+                          * exp_bloch2d.c:296-321, 628); 0 = tol */
 } mxg_solve_opts;
 
 typedef struct mxg_solver mxg_solver;

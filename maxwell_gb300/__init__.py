@@ -39,7 +39,8 @@ class SolveOpts(C.Structure):
                                                                                   ("smoother", C.c_int),
                                                                                   ("drop", C.c_double),
                                                                                   ("extrapolation", C.c_int),
-                                                                                  ("refine", C.c_int)]
+                                                                                  ("refine", C.c_int),
+                                                                                  ("nested_tol", C.c_double)]
 
 
 class ProtocolInfo(C.Structure):
@@ -384,10 +385,11 @@ class Solver:
 
     def __init__(self, kappa_fine, *, n0, L, ieigs, m, method=1, precision=1, max_nested=20,
                  max_steps=60, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1, center=1,
-                 wave=1, relative=1, tol=1e-8, smoother=1, drop=0.0, extrapolation="n", refine=0):
+                 wave=1, relative=1, tol=1e-8, smoother=1, drop=0.0, extrapolation="n", refine=0,
+                 nested_tol=0.0):
         self.o = SolveOpts(n0, L, ieigs, m, method, precision, max_nested, max_steps, prec_steps,
                            gradient_steps, smoother_steps, lift_e, center, wave, relative, tol, smoother, drop,
-                           ord(extrapolation), refine)
+                           ord(extrapolation), refine, nested_tol)
         self.n = n0 << L
         self.m, self.wave = m, wave
         k = np.ascontiguousarray(kappa_fine, np.float64)

@@ -82,6 +82,7 @@ struct mxg_solver {
   int timing;
   cudaEvent_t tev[PH_N + 1];
   double tph[PH_N];
+  double cur_tol;       /* stopping tolerance of the level being iterated */
   int prof;
   cudaEvent_t *pev;
   int *ptag;
@@ -187,6 +188,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
     return 0;
   s = calloc(1, sizeof(mxg_solver));
   s->o = *o;
+  s->cur_tol = o->tol;
   s->order = o->extrapolation == '2' ? 3 : o->extrapolation == '1' ? 2 : 1;
   if(cudaGetDevice(&s->device) != cudaSuccess) { free(s); return 0; }
   s->n0 = o->n0; s->L = o->L; s->m = m = o->m; s->K = K = o->wave;
@@ -451,7 +453,7 @@ static int vcycle_e(mxg_solver *s, int top)
 /* vcycle_node2d (node2d.c:1352-1389) on bg[top], xg[top] */
 static int vcycle_n(mxg_solver *s, int top)
 {
-  int l, i, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
+  int l, nu = s->o.smoother_steps, m = s->m, K = s->K, pg = s->pg;
   for(l = top; l > 0; l--) {
     int n = s->n[l];
     TRY(node_smooth(s, l, 0, nu));
@@ -612,7 +614,7 @@ static int converged_k(const mxg_solver *s, int k)
 {
   int i;
   for(i = 0; i < s->o.ieigs; i++)
-    if(!(s->h_res[k * s->m + i] <= s->o.tol))
+    if(!(s->h_res[k * s->m + i] <= s->cur_tol))
       return 0;
   return 1;
 }
@@ -651,7 +653,7 @@ static int ritz_body(mxg_solver *s, int l)
                     s->gscratch_bytes, s->st));
   s->launches++;   /* the reduction of the partial sums */
   prof_end(s, on);
-  L_(mxk_select_columns(ns, m, K, s->stats, s->mu, s->o.tol, s->o.relative, s->all_columns, s->sel, s->st));
+  L_(mxk_select_columns(ns, m, K, s->stats, s->mu, s->cur_tol, s->o.relative, s->all_columns, s->sel, s->st));
   if(tm) cudaEventRecord(s->tev[PH_RR], s->st);
   L_(mxk_rayleigh_ritz(ns, m, K, s->ga, s->gm, s->sel, s->rb.drop, s->rb.theta_min, s->coef, s->theta, s->info,
                        s->rwork, s->st));
@@ -744,6 +746,9 @@ static int block_step(mxg_solver *s, int l, int *have_p)
 static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
 {
   int step, k, have_p = 0, all;
+  /* the tolerance of this level: the nested iteration's own below the
+   * finest level (fixed per level, so the level's Ritz graph may keep it) */
+  s->cur_tol = l < s->L && s->o.nested_tol > 0.0 ? s->o.nested_tol : s->o.tol;
   for(k = 0; k < s->K; k++) s->h_steps[k] = 0;
   TRY(residual(s, l, 1));
   for(step = 0; step < maxsteps; step++) {
