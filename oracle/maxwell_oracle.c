@@ -1221,6 +1221,7 @@ typedef struct {
   int l, n;            /* current level and its intervals */
   long len;            /* 2 n^2 */
   cx *t1, *t2, *tn;    /* scratch (edge, edge, node) */
+  double tol;          /* stopping tolerance of the current level */
 } ctx_t;
 
 /* k = 0 up to rounding (the reference tests xfactor == 1.0 and yfactor ==
@@ -1415,7 +1416,7 @@ lobpcg_step(ctx_t *c, block_t *B)
     idx[na++] = i;
   for(j = 1; j < ns / m; j++)
     for(i = 0; i < m; i++)
-      if(B->res[i] > o->tol)
+      if(B->res[i] > c->tol)
         idx[na++] = j * m + i;
   sa = malloc(sizeof(cx) * na * na); sm = malloc(sizeof(cx) * na * na);
   sc = malloc(sizeof(cx) * na * m);
@@ -1476,7 +1477,8 @@ iterate(ctx_t *c, block_t *B, int maxsteps)
 {
   int k;
   B->have_p = 0;
-  for(k = 0; k < maxsteps && maxres(B, c->o->ieigs) > c->o->tol; k++) {
+  c->tol = c->l < c->o->L && c->o->nested_tol > 0.0 ? c->o->nested_tol : c->o->tol;
+  for(k = 0; k < maxsteps && maxres(B, c->o->ieigs) > c->tol; k++) {
     int info = c->o->method ? lobpcg_step(c, B) : pinvit_step(c, B);
     if(info)
       return -(k + 1);

@@ -110,6 +110,7 @@ typedef struct {
   int wave;              /* k-points solved together; wave w starts from wave w-1 */
   int relative;          /* 0 absolute defect (reference), 1 relative residual */
   double tol;
+  double nested_tol;     /* tolerance of the nested iteration's coarser levels; 0 = tol */
 } om_opts;
 
 int om_bloch_solve(const om_opts *o, const double *kappa_fine,

@@ -283,15 +283,15 @@ class Oracle:
     # ---- solver ----
     def bloch_solve(self, kappa_fine, factors, *, n0, L, ieigs, m, method=0, max_nested=20,
                     max_steps=40, prec_steps=2, gradient_steps=5, smoother_steps=2, lift_e=1,
-                    center=1, extrapolation="2", wave=1, relative=1, tol=1e-8,
+                    center=1, extrapolation="2", wave=1, relative=1, tol=1e-8, nested_tol=0.0,
                     want_vectors=False, want_times=False):
         class Opts(C.Structure):
             _fields_ = [(f, C.c_int) for f in (
                 "n0", "L", "ieigs", "m", "method", "max_nested", "max_steps", "prec_steps",
                 "gradient_steps", "smoother_steps", "lift_e", "center", "extrapolation", "wave",
-                "relative")] + [("tol", C.c_double)]
+                "relative")] + [("tol", C.c_double), ("nested_tol", C.c_double)]
         o = Opts(n0, L, ieigs, m, method, max_nested, max_steps, prec_steps, gradient_steps,
-                 smoother_steps, lift_e, center, ord(extrapolation), wave, relative, tol)
+                 smoother_steps, lift_e, center, ord(extrapolation), wave, relative, tol, nested_tol)
         factors = np.asarray(factors, np.complex128)
         nk = factors.shape[0]
         xfs = np.ascontiguousarray(factors[:, 0])
