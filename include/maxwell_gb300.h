@@ -209,6 +209,10 @@ int gsbackward_node2d_gpu(mxg_field alpha, const node2d_gpu *b, node2d_gpu *x);
 int gssymm_node2d_gpu(mxg_field alpha, const node2d_gpu *b, node2d_gpu *x);
 int prolongation_node2d_gpu(mxg_field alpha, const node2d_gpu *c, node2d_gpu *f);
 int restriction_node2d_gpu(mxg_field alpha, const node2d_gpu *f, node2d_gpu *c);
+/* no reference counterpart: c = restriction of (b - alpha L x), the node
+ * V-cycle's residual and restriction (node2d.c:1352-1389) in one pass, c
+ * overwritten */
+int residual_restriction_node2d_gpu(mxg_field alpha, const node2d_gpu *b, const node2d_gpu *x, node2d_gpu *c);
 int gradient_node2d_gpu(mxg_field alpha, const node2d_gpu *x, edge2d_gpu *y);
 int adjgradient_node2d_gpu(mxg_field alpha, const edge2d_gpu *x, node2d_gpu *y);
 int vcycle_node2d_gpu(int L, int nu, const matrix_gpu *Ac, node2d_gpu **b, node2d_gpu **x,

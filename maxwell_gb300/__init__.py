@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
             "gssymm_node2d_gpu": (I, [Field, P, P]),
             "prolongation_node2d_gpu": (I, [Field, P, P]),
             "restriction_node2d_gpu": (I, [Field, P, P]),
+            "residual_restriction_node2d_gpu": (I, [Field, P, P, P]),
             "gradient_node2d_gpu": (I, [Field, P, P]),
             "adjgradient_node2d_gpu": (I, [Field, P, P]),
             "vcycle_node2d_gpu": (I, [I, I, P, P, P, P]),

@@ -605,6 +605,15 @@ int prolongation_node2d_gpu(mxg_field alpha, const node2d_gpu *c, node2d_gpu *f)
   return mxk_node_prolong(c->gr->n, c->m, c->gr->K, f->gr->ph, creal_(alpha), c->prec, c->d, f->d, f->gr->st);
 }
 
+int residual_restriction_node2d_gpu(mxg_field alpha, const node2d_gpu *b, const node2d_gpu *x, node2d_gpu *c)
+{
+  if(x->gr->n != 2 * c->gr->n || x->m != c->m || b->m != x->m || x->prec != c->prec || b->prec != x->prec
+     || b->gr->n != x->gr->n)
+    return MXG_EINVAL;
+  return mxk_node_residual_restrict(c->gr->n, c->m, c->gr->K, x->gr->ph, creal_(alpha), c->prec, x->d, b->d, c->d,
+                                    x->gr->st);
+}
+
 int restriction_node2d_gpu(mxg_field alpha, const node2d_gpu *f, node2d_gpu *c)
 {
   if(f->gr->n != 2 * c->gr->n || c->m != f->m || c->prec != f->prec) return MXG_EINVAL;

@@ -81,6 +81,9 @@ int mxk_node_apply(int n, int m, int K, const double *phases, double alpha, doub
                    int prec, const void *x, const void *yin, void *y, mx_stream s);
 int mxk_node_gs(int n, int m, int K, const double *phases, double alpha, int dir,
                 int prec, const void *b, void *x, mx_stream s);
+/* c (level nc) = restriction of (b - alpha L x) on level 2 nc, written */
+int mxk_node_residual_restrict(int nc, int m, int K, const double *phases, double alpha, int prec,
+                               const void *x, const void *b, void *c, mx_stream s);
 /* one node GS sweep (dir 0 forward, 1 backward) read from x, written to y
  * (tiled, three launches); for c64 blocks with m % 4 == 0 and n >= 128 */
 int mxk_node_gs_oop_ok(int n, int m, int prec);

@@ -297,6 +297,8 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
          mxk_edge_prolong(n / 2, m, K, ph, 1.0, MX_C64, bc, x, st));
     TIME("node_residual_c64", 3 * V8 * s8, 1,
          mxk_node_apply(n, m, K, ph, -1.0, 1.0, MX_C64, nx, nb, nd, st));
+    TIME("node_residual_restrict_c64", (2 * V8 + V8 / 4) * s8, 1,
+         mxk_node_residual_restrict(n / 2, m, K, ph, 1.0, MX_C64, nx, nb, nbc, st));
     TIME("node_gs_forward_c64", 3 * V8 * s8, 4,
          mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st));
     {

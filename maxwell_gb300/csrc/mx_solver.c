@@ -457,9 +457,8 @@ static int vcycle_n(mxg_solver *s, int top)
   for(l = top; l > 0; l--) {
     int n = s->n[l];
     TRY(node_smooth(s, l, 0, nu));
-    L_(mxk_node_apply(n, m, K, s->ph, -1.0, 1.0, pg, s->xg[l], s->bg[l], s->dg[l], s->st));
-    L_(mxk_zero(pg, s->bg[l - 1], nlen(s, l - 1), s->st));
-    L_(mxk_node_restrict(n / 2, m, K, s->ph, 1.0, pg, s->dg[l], s->bg[l - 1], s->st));
+    /* the residual and its restriction in one kernel (written, not added) */
+    L_(mxk_node_residual_restrict(n / 2, m, K, s->ph, 1.0, pg, s->xg[l], s->bg[l], s->bg[l - 1], s->st));
     L_(mxk_zero(pg, s->xg[l - 1], nlen(s, l - 1), s->st));
   }
   L_(mxk_coarse_apply(s->n0 * s->n0, m, K, s->an_inv, s->an_inv_f, pg, s->bg[0], s->xg[0], s->st));

@@ -210,6 +210,13 @@ def test_transfers_node_ops_gradient(oracle, setup, prec):
     mx.check(mx.lib().restriction_node2d_gpu(mx.fz(1.0), nv.h, nvc.h))
     want = np.array([[oracle.restrict_node(nc, *FACTORS[k], 1.0, v_[k, i], vc[k, i]) for i in range(m)] for k in range(K)])
     assert rel(nvc.get(), want) < tol
+    # the V-cycle's fused residual + restriction: c = R(b - 0.8 L x), c overwritten
+    nw.put(w_)
+    mx.check(mx.lib().residual_restriction_node2d_gpu(mx.fz(0.8), nw.h, nv.h, nvc.h))
+    want = np.array([[oracle.restrict_node(nc, *FACTORS[k], 1.0,
+                                           oracle.addeval_node(n, *FACTORS[k], -0.8, v_[k, i], w_[k, i]),
+                                           np.zeros(nc * nc)) for i in range(m)] for k in range(K)])
+    assert rel(nvc.get(), want) < tol
     ef.put(f)
     mx.check(mx.lib().gradient_node2d_gpu(mx.fz(-1.0), nv.h, ef.h))
     want = np.array([[oracle.gradient(n, *FACTORS[k], -1.0, v_[k, i], f[k, i]) for i in range(m)] for k in range(K)])
