@@ -184,21 +184,24 @@ def cpu_path_solve(threads: int, kap, fac):
 
 def cpu_baseline(kap, fac, threads: int, lam_gpu) -> dict:
     """A bounded sample of the same workload on the host cores: the first
-    three k-points of the path solved to the relative residual 1e-8 (one cold
-    start, two warm starts).  The rate of the whole 32-point path is the cold
-    k-point plus 31 warm ones at the sampled mean; only the number of
-    k-points is extrapolated.  The sample's eigenvalues are also the CPU FP64
-    check of the GPU's at the same k-points."""
+    three k-points of the path solved to the relative residual 1e-8 -- Gamma
+    and the point after it from cold starts (the Gamma block lacks the two
+    lowest bands of k != 0, so the port starts the next point cold), the
+    third warm-started.  The rate of the whole 32-point path is those two
+    cold k-points plus 30 warm ones at the sampled warm time; only the
+    number of k-points is extrapolated.  The sample's eigenvalues are also
+    the CPU FP64 check of the GPU's at the same k-points."""
     nks = 3
     lam, steps, res, secs = cpu_path_solve(threads, kap, fac[:nks])
-    t_cold, t_warm = float(secs[0]), float(np.mean(secs[1:]))
-    per_path = t_cold + (NK - 1) * t_warm
+    t_cold, t_warm = float(secs[0] + secs[1]), float(np.mean(secs[2:]))
+    per_path = t_cold + (NK - 2) * t_warm
     diff = np.abs(lam_gpu[:nks, :IEIGS] - lam[:, :IEIGS]) / np.abs(lam[:, :IEIGS])
     return {"value": NK / per_path, "unit": "k-points/s", "cores": threads, "kind": "port",
             "sample": (f"the first {nks} k-points of the 512^2 path solved to relative residual 1e-8 by the "
-                       f"oracle port: cold start {t_cold:.1f} s ({int(steps[0])} LOBPCG steps after the nested "
-                       f"iteration), warm starts {', '.join(f'{t:.1f}' for t in secs[1:])} s "
-                       f"({', '.join(str(int(q)) for q in steps[1:])} steps); 32-point path = 1 cold + 31 warm"),
+                       f"oracle port: cold starts at Gamma and the next point {secs[0]:.1f}, {secs[1]:.1f} s "
+                       f"({int(steps[0])}, {int(steps[1])} LOBPCG steps after the nested iteration), warm start "
+                       f"{', '.join(f'{t:.1f}' for t in secs[2:])} s "
+                       f"({', '.join(str(int(q)) for q in steps[2:])} steps); 32-point path = 2 cold + 30 warm"),
             "measured_seconds": [float(t) for t in secs], "steps": [int(q) for q in steps],
             "max_rel_eig_diff_gpu_vs_cpu": float(diff.max()),
             "max_rel_residual_cpu": float(res[:, :IEIGS].max())}
@@ -382,7 +385,9 @@ def run_reference(args):
     start (coarse eigenproblem, nested iteration), every later one
     warm-started by second-order Rayleigh-Ritz extrapolation.  Each step is
     one k-point solved to the relative residual 1e-8: the first --warmup
-    k-points are untimed, the next --steps are timed one by one."""
+    k-points are untimed, the next --steps are timed one by one.  (The point
+    after Gamma starts cold: the Gamma block lacks the two lowest bands of
+    every k != 0.)"""
     ws, rank = dist_env()
     if rank != 0:
         return
@@ -405,7 +410,7 @@ def run_reference(args):
                                        f"untimed ones, each solved to relative residual 1e-8 and timed on its "
                                        f"own (block steps {', '.join(str(int(q)) for q in steps[args.warmup:])})")},
            "e2e": {"value": v, "unit": "k-points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "max_rel_residual": float(res[:, :IEIGS].max())}
+           "max_rel_residual": float(res[args.warmup:, :IEIGS].max())}
     print(json.dumps(out), flush=True)
 
 

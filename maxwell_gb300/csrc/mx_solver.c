@@ -83,6 +83,7 @@ struct mxg_solver {
   cudaEvent_t tev[PH_N + 1];
   double tph[PH_N];
   double cur_tol;       /* stopping tolerance of the level being iterated */
+  int wave_gamma;       /* the current wave holds Gamma */
   int prof;
   cudaEvent_t *pev;
   int *ptag;
@@ -320,6 +321,8 @@ static int set_bloch(mxg_solver *s, int K, const mxg_field *xf, const mxg_field 
     s->h_ph[4 * k + 2] = creal(yf[q]); s->h_ph[4 * k + 3] = cimag(yf[q]);
     g[k] = is_gamma(xf[q], yf[q]);
   }
+  s->wave_gamma = 0;
+  for(k = 0; k < K; k++) s->wave_gamma |= g[k];
   mxk_phase_fill(s->K, s->h_ph);
   e = (int) cudaMemcpyAsync(s->ph, s->h_ph, mxk_phase_bytes(s->K), cudaMemcpyHostToDevice, s->st);
   if(!e) e = (int) cudaMemcpyAsync(s->gamma, g, sizeof(int) * s->K, cudaMemcpyHostToDevice, s->st);
@@ -917,11 +920,14 @@ int mxg_bloch_solve(mxg_solver *s, int nk, const mxg_field *xf, const mxg_field 
   s->restarts = 0;
   s->have_prev = 0;   /* every call starts cold; later waves of this call start warm */
   for(w = 0; w * K < nk; w++) {
-    int k0 = w * K, Ka = nk - k0 < K ? nk - k0 : K;
+    int k0 = w * K, Ka = nk - k0 < K ? nk - k0 : K, after_gamma = s->wave_gamma;
     TRY(set_bloch(s, Ka, xf + k0, yf + k0));
     TRY((int) cudaEventRecord(s->ev0, s->st));
     TRY(factor_coarse(s));
-    if(!s->have_prev || s->K_prev != K || s->o.extrapolation == 'c') {
+    /* a wave after one holding Gamma starts cold: the Gamma block is centred
+     * and lacks the two lowest bands of every k != 0 (they tend to the
+     * constant fields that centring removes) */
+    if(!s->have_prev || s->K_prev != K || s->o.extrapolation == 'c' || after_gamma) {
       double tc = now_s();
       TRY(cold_start(s, Ka));
       if(s->timing) fprintf(stderr, "wave %d: cold start incl. finest-level steps %.3f s\n", w, now_s() - tc);
