@@ -62,6 +62,7 @@ struct mxg_solver {
   void *ae_inv_f, *an_inv_f;         /* their c64 roundings (FP32 solves) */
   void *E, *En, *P, *Pn;
   void *Eprev[3];                    /* eigenvectors of the last three waves, newest first */
+  void *Eref;                        /* the block before the refinement sweep (refine only) */
   double *ga, *gm, *coef, *theta, *rwork, *gscratch, *mu, *stats;
   size_t gscratch_bytes;
   int *sel, *info;
@@ -153,7 +154,7 @@ void mxg_solver_free(mxg_solver *s)
   }
   cudaFree(s->ph); cudaFree(s->ph2); cudaFree(s->gamma); cudaFree(s->ae_inv); cudaFree(s->an_inv); cudaFree(s->ae_inv_f); cudaFree(s->an_inv_f);
   cudaFree(s->E); cudaFree(s->En); cudaFree(s->P); cudaFree(s->Pn);
-  cudaFree(s->Eprev[0]); cudaFree(s->Eprev[1]); cudaFree(s->Eprev[2]);
+  cudaFree(s->Eprev[0]); cudaFree(s->Eprev[1]); cudaFree(s->Eprev[2]); cudaFree(s->Eref);
   cudaFree(s->ga); cudaFree(s->gm); cudaFree(s->coef); cudaFree(s->theta); cudaFree(s->rwork);
   cudaFree(s->gscratch); cudaFree(s->mu); cudaFree(s->stats); cudaFree(s->sel); cudaFree(s->info);
   cudaFree(s->cA); cudaFree(s->cM); cudaFree(s->ccoef); cudaFree(s->ctheta); cudaFree(s->cwork);
@@ -257,6 +258,7 @@ mxg_solver *mxg_solver_new(const mxg_solve_opts *o, const double *kappa_fine)
      || dalloc(&s->Eprev[0], elen(s, o->L) * es_e)
      || (s->order > 1 && dalloc(&s->Eprev[1], elen(s, o->L) * es_e))
      || (s->order > 2 && dalloc(&s->Eprev[2], elen(s, o->L) * es_e))
+     || (o->refine && dalloc(&s->Eref, elen(s, o->L) * es_e))
      || dalloc(&s->P, elen(s, o->L) * es_g) || dalloc(&s->Pn, elen(s, o->L) * es_g)
      || dalloc((void **) &s->ga, sizeof(double) * 2 * ns * ns * K) || dalloc((void **) &s->gm, sizeof(double) * 2 * ns * ns * K)
      || dalloc((void **) &s->coef, sizeof(double) * 2 * ns * m * K) || dalloc((void **) &s->theta, sizeof(double) * m * K)
@@ -732,7 +734,10 @@ static int block_step(mxg_solver *s, int l, int *have_p)
     nb = *have_p ? 3 : 2;
     /* mu = 1 + lambda: pairs with lambda <= 1e-7 are gradient (null-space)
      * modes that the search directions' rounding can expose */
-    TRY(ritz(s, l, nb, pr, pp, 1, drop_tol(s), 1.0 + 1e-7));
+    /* the refinement step's basis holds the search columns of converged
+     * pairs too, nearly dependent on their eigenvectors: it drops columns
+     * more readily */
+    TRY(ritz(s, l, nb, pr, pp, 1, s->all_columns && drop_tol(s) < 1e-4 ? 1e-4 : drop_tol(s), 1.0 + 1e-7));
     if(tm) cudaEventRecord(s->tev[PH_LIFTE], s->st);
     *have_p = 1;
     if(s->o.lift_e) {
@@ -790,11 +795,39 @@ static int iterate(mxg_solver *s, int l, int maxsteps, int K_active)
     if(!converged_k(s, k)) s->h_steps[k] = maxsteps;
   if(l == s->L && s->o.refine) {
     /* the refinement sweep: one more block step with every column of the
-     * search blocks in the Ritz basis, then the residuals again */
+     * search blocks in the Ritz basis, then the residuals again.  A k-point
+     * whose wanted pairs come out worse keeps its block from before (the
+     * sweep is kept per k-point, on the device) */
+    double *before = malloc(sizeof(double) * 2 * s->K * s->m);
+    int worse = 0, e;
+    if(!before) return MXG_ENOMEM;
+    memcpy(before, s->h_res, sizeof(double) * s->K * s->m);
+    memcpy(before + s->K * s->m, s->h_rq, sizeof(double) * s->K * s->m);
+    L_(mxk_convert(s->pe, s->E, s->pe, s->Eref, elen(s, l), s->st));
     s->all_columns = 1;
     TRY(block_step(s, l, &have_p));
     s->all_columns = 0;
-    TRY(residual(s, l, 1));
+    e = residual(s, l, 1);
+    if(e && e != MXG_ECONV) { free(before); return e; }
+    for(k = 0; k < K_active; k++) {
+      double b0 = 0.0, b1 = 0.0;
+      int i;
+      for(i = 0; i < s->o.ieigs; i++) {
+        double r0 = before[k * s->m + i], r1 = s->h_res[k * s->m + i];
+        if(r0 > b0) b0 = r0;
+        if(!(r1 <= b1)) b1 = r1;   /* NaN counts as worst */
+      }
+      if(e == MXG_ECONV || !(b1 <= b0)) {
+        /* restore the pre-sweep block of this k-point and its statistics */
+        const size_t slot = elen(s, l) / s->K * mxk_elem_size(s->pe);
+        worse = (int) cudaMemcpyAsync((char *) s->E + k * slot, (const char *) s->Eref + k * slot, slot,
+                                      cudaMemcpyDeviceToDevice, s->st);
+        memcpy(s->h_res + k * s->m, before + k * s->m, sizeof(double) * s->m);
+        memcpy(s->h_rq + k * s->m, before + s->K * s->m + k * s->m, sizeof(double) * s->m);
+        if(worse) { free(before); return worse; }
+      }
+    }
+    free(before);
   }
   return 0;
 }
