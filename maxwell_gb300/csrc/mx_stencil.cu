@@ -1085,6 +1085,9 @@ __global__ void k_axpy(Sc are, Sc aim, const SX* __restrict__ x, SY* __restrict_
 // mean of each plane of each (k, v), in two passes: partial sums of a chunk
 // of sites per block added atomically into acc[(k*2+p)*m+v] (re, im), then
 // the subtraction; only k-points whose flag is set are touched
+template <typename S> struct CenterAcc { using T = dd; };
+template <> struct CenterAcc<double2> { using T = double; };
+
 template <typename S, typename R>
 __global__ void k_center_sum(int n, int m, int K, const int* __restrict__ gamma, const S* __restrict__ x,
                              double* acc) {
@@ -1092,16 +1095,20 @@ __global__ void k_center_sum(int n, int m, int K, const int* __restrict__ gamma,
   if (!gamma[k]) return;
   Lay L{n, m, K};
   int v = threadIdx.x, row = threadIdx.y, rows = blockDim.y;
-  double are = 0.0, aim = 0.0;
+  // float-float sums on the FP32 pipes for c64 and float-float vectors
+  // (GB300 adds in FP64 at a small fraction of that rate), FP64 sums for
+  // FP64 vectors; FP64 for the block's partial sums
+  using A = typename CenterAcc<S>::T;
+  A are = Real<A>::zero(), aim = Real<A>::zero();
   for (int s = blockIdx.x * rows + row; s < n * n; s += gridDim.x * rows) {
-    cx<double> val = Store<S, double>::ld(x + L.edge(k, p, 0, 0, v) + (size_t) s * m);
+    cx<A> val = Store<S, A>::ld(x + L.edge(k, p, 0, 0, v) + (size_t) s * m);
     are += val.re;
     aim += val.im;
   }
   __shared__ double sre[256], sim[256];
   int t = threadIdx.y * blockDim.x + threadIdx.x;
-  sre[t] = are;
-  sim[t] = aim;
+  sre[t] = Real<A>::to_double(are);
+  sim[t] = Real<A>::to_double(aim);
   __syncthreads();
   if (threadIdx.y == 0) {
     double tr = 0.0, ti = 0.0;
@@ -1340,7 +1347,7 @@ template <typename S, typename R>
 static int L_center(int n, int m, int K, const int* gamma, void* x, double* acc, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(double) * 4 * (size_t) K * m, st);
   if (e) return (int) e;
-  unsigned chunks = (unsigned) ((n * n + 4095) / 4096);
+  unsigned chunks = (unsigned) ((n * n + 1023) / 1024);
   k_center_sum<S, R><<<dim3(chunks, 2 * K), blk2(m), 0, st>>>(n, m, K, gamma, (const S*) x, acc);
   MX_CHECK_LAUNCH();
   unsigned rows = 256 / m;
