@@ -672,45 +672,73 @@ __global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph,
 // c(ci, cj) = sum of d over the 3 x 3 fine nodes around (2ci, 2cj) with
 // weights 1, 1/2, 1/4, where d = b - alpha L x is formed from the 5 x 5
 // window of x around them; the coarse vector is written, not accumulated.
-// A thread per (coarse node, vector); neighbouring threads share their
-// windows through L1, so x and b come from DRAM once and d never goes
-// there: 2.25 fine arrays of traffic against 4.25 for the two kernels.
+// A thread per (coarse column, strip of RR_CH coarse rows, vector) walks up
+// its strip: it keeps the fine rows of x and the row of d that the next
+// coarse node shares with the last one in registers, so a coarse node costs
+// two new rows of x (10 loads), two of b (6) and two rows of d (6 values)
+// instead of the whole 5 x 5 window and nine values of d.  The threads of a
+// block take neighbouring columns and share their column halo through L1,
+// so x and b come from DRAM once and d never goes there: 2.25 fine arrays
+// of traffic against 4.25 for the two kernels.
+constexpr int RR_CH = 8;
 template <typename S, typename R>
-__global__ void k_node_residual_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc diag, Sc off,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_node_residual_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc diag, Sc off,
                                          const S* __restrict__ x, const S* __restrict__ b, S* __restrict__ c) {
-  const int nf = 2 * nc;
-  // block (m, rows): x = vector, y = coarse node; grid.y = k-point
+  const int nf = 2 * nc, nst = (nc + RR_CH - 1) / RR_CH;
+  // block (m, columns): x = vector, y = (column, strip); grid.y = k-point
   const int k = blockIdx.y, v = threadIdx.x;
-  const int site = blockIdx.x * blockDim.y + threadIdx.y;
-  if (site >= nc * nc) return;
-  const int ci = site % nc, cj = site / nc, fi = 2 * ci, fj = 2 * cj;
+  const int s = blockIdx.x * blockDim.y + threadIdx.y;
+  if (s >= nc * nst) return;
+  const int ci = s % nc, cj0 = (s / nc) * RR_CH, cj1 = min(cj0 + RR_CH, nc), fi = 2 * ci;
   Lay Lc{nc, m, K}, Lf{nf, m, K};
   const S* xb = x + Lf.node(k, 0, 0, v);
   const S* bb = b + Lf.node(k, 0, 0, v);
   const R dg = sget<R>(diag), of = sget<R>(off), half = rc<R>(0.5f), quarter = rc<R>(0.25f);
-  cx<R> sres;
   auto body = [&](const auto& X, const auto& B) {
-    cx<R> w[5][5];
+    // x at fine columns fi-2..fi+2 of four consecutive fine rows
+    cx<R> xa[5], xm[5], xc[5], xd[5], dp[3], d0[3], dn[3];
+    auto ldx = [&](cx<R>* w, int fj) {
 #pragma unroll
-    for (int q = 0; q < 5; q++)
-#pragma unroll
-      for (int p = 0; p < 5; p++) w[q][p] = X(fi - 2 + p, fj - 2 + q);
-    // d at fine node (fi + a, fj + e), a, e in -1..1
-    auto d = [&](int a, int e) {
-      const int p = a + 2, q = e + 2;
-      const cx<R> nb = w[q][p - 1] + w[q][p + 1] + w[q - 1][p] + w[q + 1][p] + w[q - 1][p - 1] + w[q - 1][p + 1]
-                       + w[q + 1][p - 1] + w[q + 1][p + 1];
-      return B(fi + a, fj + e) - (scal(dg, w[q][p]) + scal(of, nb));
+      for (int p = 0; p < 5; p++) w[p] = X(fi - 2 + p, fj);
     };
-    sres = d(0, 0) + scal(half, d(-1, 0) + d(1, 0) + d(0, -1) + d(0, 1))
-           + scal(quarter, d(-1, -1) + d(1, -1) + d(-1, 1) + d(1, 1));
+    // d at fine columns fi-1..fi+1 of row fj, from x rows fj-1 (u), fj (w), fj+1 (l)
+    auto drow = [&](const cx<R>* u, const cx<R>* w, const cx<R>* l, int fj, cx<R>* d) {
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const int p = a + 1;
+        const cx<R> nb = w[p - 1] + w[p + 1] + u[p] + l[p] + u[p - 1] + u[p + 1] + l[p - 1] + l[p + 1];
+        d[a] = B(fi - 1 + a, fj) - (scal(dg, w[p]) + scal(of, nb));
+      }
+    };
+    int fj = 2 * cj0;
+    ldx(xc, fj - 2);
+    ldx(xa, fj - 1);
+    ldx(xm, fj);
+    drow(xc, xa, xm, fj - 1, dp);
+#pragma unroll 1
+    for (int cj = cj0; cj < cj1; cj++, fj += 2) {
+      ldx(xc, fj + 1);
+      ldx(xd, fj + 2);
+      drow(xa, xm, xc, fj, d0);
+      drow(xm, xc, xd, fj + 1, dn);
+      const cx<R> sres = d0[1] + scal(half, d0[0] + d0[2] + dp[1] + dn[1])
+                         + scal(quarter, dp[0] + dp[2] + dn[0] + dn[2]);
+      Store<S, R>::st(c + Lc.node(k, cj, ci, v), sres);
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        xa[p] = xc[p];
+        xm[p] = xd[p];
+      }
+#pragma unroll
+      for (int a = 0; a < 3; a++) dp[a] = dn[a];
+    }
   };
-  if (ci > 0 && cj > 0 && ci < nc - 1 && cj < nc - 1) body(NAccI<S, R>{xb, nf, m}, NAccI<S, R>{bb, nf, m});
+  // the strip's x rows run from 2 cj0 - 2 to 2 cj1, its columns from fi-2 to fi+2
+  if (ci > 0 && ci < nc - 1 && cj0 > 0 && cj1 < nc) body(NAccI<S, R>{xb, nf, m}, NAccI<S, R>{bb, nf, m});
   else {
     const Seam<R> seam = seam_load<R>(ph, K, k, nf);
     body(NAcc<S, R>{xb, nf, m, seam}, NAcc<S, R>{bb, nf, m, seam});
   }
-  Store<S, R>::st(c + Lc.node(k, cj, ci, v), sres);
 }
 
 template <typename S, typename R>
@@ -1380,7 +1408,8 @@ static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, i
 template <typename S, typename R>
 static int L_node_residual_restrict(int nc, int m, int K, const double* ph, double alpha, const void* x,
                                    const void* b, void* c, cudaStream_t st) {
-  k_node_residual_restrict<S, R><<<grd2((size_t) nc * nc, m, K), blk2(m), 0, st>>>(
+  const size_t strips = (size_t) nc * ((nc + RR_CH - 1) / RR_CH);
+  k_node_residual_restrict<S, R><<<grd2(strips, m, K), blk2(m), 0, st>>>(
       nc, m, K, ph, make_sc(alpha * 8.0 / 3.0), make_sc(-alpha / 3.0), (const S*) x, (const S*) b, (S*) c);
   MX_CHECK_LAUNCH();
   return 0;
