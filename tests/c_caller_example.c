@@ -14,8 +14,12 @@ int solve_bloch(int n0, int L, const double *kappa, int nk,
   int e;
   o.n0 = n0; o.L = L; o.ieigs = 12; o.m = 16;
   o.method = 1;               /* LOBPCG; 0 = the reference's block PINVIT + Ritz */
-  o.precision = 1;            /* FP32 multigrid, float-float eigenvectors */
-  o.max_nested = 30; o.max_steps = 60;
+  o.precision = 1;            /* FP32 multigrid, float-float eigenvectors; 2 = FP64
+                               * eigenvectors for residuals below the float-float floor
+                               * (about 8 n^2 2^-48 / lambda: near 1e-9 at 1024^2) */
+  o.max_nested = 20; o.max_steps = 60;
+  o.nested_tol = 1e-2;        /* coarser levels of the nested iteration stop at 1e-2
+                               * (the driver's default residual rule); 0 = o.tol */
   o.prec_steps = 2; o.gradient_steps = 5; o.smoother_steps = 2;
   o.lift_e = 1; o.center = 1; o.wave = nk; o.relative = 1; o.tol = 1e-8;
   o.smoother = 1;             /* four-colour AFW; 0 = the reference's row order */
