@@ -410,14 +410,18 @@ int mxg_kernel_bench(int n, int K, int m, int reps, mxg_kbench_row *rows, int ma
 /* ---------- launch-shape autotuner (no counterpart in the reference) ---------- */
 /* Launch shapes, process-wide: the Gram's CTAs per k-point (gram_waves x
  * SMs / K), the tiled combination's CTAs (combine_ctas x SMs), the block
- * residual's sites per thread, and the tiled node Gauss-Seidel sweep's strip
- * width (positions) and band height (pairs of rows) per CTA. */
+ * residual's sites per thread, the tiled node Gauss-Seidel sweep's strip
+ * width (positions) and band height (pairs of rows) per CTA, and from which
+ * batch the node V-cycle's residual + restriction walks strips of coarse
+ * rows (coarse nodes x vectors x k-points >= 2^restrict_strip_log2) instead
+ * of taking a thread per coarse node. */
 typedef struct {
   int gram_waves;        /* 1 .. 64 */
   int combine_ctas;      /* 1 .. 16 */
   int residual_sites;    /* 1 .. 1024 */
   int node_strip;        /* 0 (the in-place row kernels), 64 or 128 */
   int node_band;         /* 1 .. 256 */
+  int restrict_strip_log2; /* 0 .. 62 (0: always strips, 62: never) */
 } mxg_tuning;
 int mxg_get_tuning(mxg_tuning *t);
 int mxg_set_tuning(const mxg_tuning *t);

@@ -212,7 +212,7 @@ def kernel_bench(n: int, K: int, m: int, reps: int = 5) -> list[dict]:
 class Tuning(C.Structure):
     """mxg_tuning: launch shapes of the block kernels."""
     _fields_ = [("gram_waves", C.c_int), ("combine_ctas", C.c_int), ("residual_sites", C.c_int),
-                ("node_strip", C.c_int), ("node_band", C.c_int)]
+                ("node_strip", C.c_int), ("node_band", C.c_int), ("restrict_strip_log2", C.c_int)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -235,8 +235,8 @@ def get_tuning() -> dict:
 
 
 def set_tuning(gram_waves: int, combine_ctas: int, residual_sites: int, node_strip: int = 0,
-               node_band: int = 16) -> None:
-    t = Tuning(gram_waves, combine_ctas, residual_sites, node_strip, node_band)
+               node_band: int = 16, restrict_strip_log2: int = 25) -> None:
+    t = Tuning(gram_waves, combine_ctas, residual_sites, node_strip, node_band, restrict_strip_log2)
     check(lib().mxg_set_tuning(C.byref(t)), "mxg_set_tuning")
 
 

@@ -92,6 +92,10 @@ int mxk_node_gs_oop(int n, int m, int K, const double *phases, double alpha, int
 /* strip width (64 or 128 positions) and band height (pairs of rows) */
 int mxk_node_gs_oop_shape(int strip, int band);
 void mxk_node_gs_oop_get_shape(int *strip, int *band);
+/* the fused node residual + restriction takes strips of coarse rows from
+ * 2^log2 (coarse node, vector, k-point) triples on (0 .. 62) */
+int mxk_node_rr_set_strips(int log2);
+int mxk_node_rr_get_strips(void);
 int mxk_node_prolong(int nc, int m, int K, const double *phases, double alpha,
                      int prec, const void *c, void *f, mx_stream s);
 int mxk_node_restrict(int nc, int m, int K, const double *phases, double alpha,

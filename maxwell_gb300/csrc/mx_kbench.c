@@ -66,6 +66,7 @@ int mxg_get_tuning(mxg_tuning *t)
   t->combine_ctas = q.combine_ctas;
   t->residual_sites = q.residual_sites;
   mxk_node_gs_oop_get_shape(&t->node_strip, &t->node_band);
+  t->restrict_strip_log2 = mxk_node_rr_get_strips();
   return 0;
 }
 
@@ -76,6 +77,7 @@ int mxg_set_tuning(const mxg_tuning *t)
   q.gram_waves = t->gram_waves;
   q.combine_ctas = t->combine_ctas;
   q.residual_sites = t->residual_sites;
+  if(t->restrict_strip_log2 < 0 || t->restrict_strip_log2 > 62) return MXG_EINVAL;
   mxk_get_tuning(&old);
   mxk_node_gs_oop_get_shape(&s0, &b0);
   if(mxk_set_tuning(&q)) return MXG_EINVAL;
@@ -83,7 +85,7 @@ int mxg_set_tuning(const mxg_tuning *t)
     mxk_set_tuning(&old);
     return MXG_EINVAL;
   }
-  return 0;
+  return mxk_node_rr_set_strips(t->restrict_strip_log2) ? MXG_EINVAL : 0;
 }
 
 int mxg_autotune(int n, int K, int m, int reps, mxg_tuning *chosen)
@@ -103,6 +105,7 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
   size_t nn = (size_t) n * n, ne = 2 * nn, q;
   size_t E8 = ne * m * K, V8 = nn * m * K;       /* entries per edge / node block */
   int err = 0, nr = 0, k, it;
+  const int rr0 = mxk_node_rr_get_strips();
   double *h_ph = 0, *kd = 0, *ph = 0, *theta = 0, *ga = 0, *gm = 0, *coef = 0, *stats = 0, *acc = 0, *gs = 0;
   double *hk = 0, *hmu = 0, *mu = 0;
   float *kf = 0, *kdd = 0, *hkf = 0, *hkdd = 0;
@@ -244,6 +247,7 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
     tune->gram_waves = base.gram_waves;
     tune->combine_ctas = base.combine_ctas;
     tune->residual_sites = base.residual_sites;
+    tune->restrict_strip_log2 = mxk_node_rr_get_strips();
     mxk_node_gs_oop_get_shape(&tune->node_strip, &tune->node_band);
     {
       /* the node sweep: the in-place row kernels (strip 0) against the
@@ -297,8 +301,16 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
          mxk_edge_prolong(n / 2, m, K, ph, 1.0, MX_C64, bc, x, st));
     TIME("node_residual_c64", 3 * V8 * s8, 1,
          mxk_node_apply(n, m, K, ph, -1.0, 1.0, MX_C64, nx, nb, nd, st));
+    /* both forms of the fused residual + restriction, whatever the current
+     * batch threshold (restored at the end): the strips, then a thread per
+     * coarse node */
+    mxk_node_rr_set_strips(0);
     TIME("node_residual_restrict_c64", (2 * V8 + V8 / 4) * s8, 1,
          mxk_node_residual_restrict(n / 2, m, K, ph, 1.0, MX_C64, nx, nb, nbc, st));
+    mxk_node_rr_set_strips(62);
+    TIME("node_residual_restrict_site_c64", (2 * V8 + V8 / 4) * s8, 1,
+         mxk_node_residual_restrict(n / 2, m, K, ph, 1.0, MX_C64, nx, nb, nbc, st));
+    mxk_node_rr_set_strips(rr0);
     TIME("node_gs_forward_c64", 3 * V8 * s8, 4,
          mxk_node_gs(n, m, K, ph, 1.0, 0, MX_C64, nb, nx, st));
     {
@@ -352,6 +364,7 @@ static int run(int n, int K, int m, int reps, mxg_kbench_row *rows, int maxrows,
 #undef TIME
 
 done:
+  mxk_node_rr_set_strips(rr0);
   cudaFree(kd); cudaFree(kf); cudaFree(kdd); cudaFree(afw); cudaFree(ph); cudaFree(mu); cudaFree(gamma);
   cudaFree(theta); cudaFree(ga); cudaFree(gm); cudaFree(coef); cudaFree(cw); cudaFree(stats); cudaFree(acc);
   cudaFree(gs); cudaFree(E); cudaFree(out); cudaFree(X); cudaFree(P); cudaFree(r); cudaFree(b); cudaFree(x);

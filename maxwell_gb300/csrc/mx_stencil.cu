@@ -672,14 +672,54 @@ __global__ void k_node_apply(int n, int m, int K, const double* __restrict__ ph,
 // c(ci, cj) = sum of d over the 3 x 3 fine nodes around (2ci, 2cj) with
 // weights 1, 1/2, 1/4, where d = b - alpha L x is formed from the 5 x 5
 // window of x around them; the coarse vector is written, not accumulated.
-// A thread per (coarse column, strip of RR_CH coarse rows, vector) walks up
-// its strip: it keeps the fine rows of x and the row of d that the next
-// coarse node shares with the last one in registers, so a coarse node costs
-// two new rows of x (10 loads), two of b (6) and two rows of d (6 values)
-// instead of the whole 5 x 5 window and nine values of d.  The threads of a
-// block take neighbouring columns and share their column halo through L1,
-// so x and b come from DRAM once and d never goes there: 2.25 fine arrays
-// of traffic against 4.25 for the two kernels.
+// Neighbouring threads share their windows through L1, so x and b come from
+// DRAM once and d never goes there: 2.25 fine arrays of traffic against
+// 4.25 for the two kernels.  Two forms: a thread per (coarse node, vector)
+// (k_node_residual_restrict_site), and for large batches a thread per
+// (coarse column, strip of RR_CH coarse rows, vector) that walks up its
+// strip keeping the fine rows of x and the row of d that the next coarse
+// node shares with the last one in registers, so a coarse node costs two
+// new rows of x (10 loads), two of b (6) and two rows of d (6 values)
+// instead of the whole 5 x 5 window and nine values of d.
+template <typename S, typename R>
+__global__ void k_node_residual_restrict_site(int nc, int m, int K, const double* __restrict__ ph, Sc diag,
+                                              Sc off, const S* __restrict__ x, const S* __restrict__ b,
+                                              S* __restrict__ c) {
+  const int nf = 2 * nc;
+  // block (m, rows): x = vector, y = coarse node; grid.y = k-point
+  const int k = blockIdx.y, v = threadIdx.x;
+  const int site = blockIdx.x * blockDim.y + threadIdx.y;
+  if (site >= nc * nc) return;
+  const int ci = site % nc, cj = site / nc, fi = 2 * ci, fj = 2 * cj;
+  Lay Lc{nc, m, K}, Lf{nf, m, K};
+  const S* xb = x + Lf.node(k, 0, 0, v);
+  const S* bb = b + Lf.node(k, 0, 0, v);
+  const R dg = sget<R>(diag), of = sget<R>(off), half = rc<R>(0.5f), quarter = rc<R>(0.25f);
+  cx<R> sres;
+  auto body = [&](const auto& X, const auto& B) {
+    cx<R> w[5][5];
+#pragma unroll
+    for (int q = 0; q < 5; q++)
+#pragma unroll
+      for (int p = 0; p < 5; p++) w[q][p] = X(fi - 2 + p, fj - 2 + q);
+    // d at fine node (fi + a, fj + e), a, e in -1..1
+    auto d = [&](int a, int e) {
+      const int p = a + 2, q = e + 2;
+      const cx<R> nb = w[q][p - 1] + w[q][p + 1] + w[q - 1][p] + w[q + 1][p] + w[q - 1][p - 1] + w[q - 1][p + 1]
+                       + w[q + 1][p - 1] + w[q + 1][p + 1];
+      return B(fi + a, fj + e) - (scal(dg, w[q][p]) + scal(of, nb));
+    };
+    sres = d(0, 0) + scal(half, d(-1, 0) + d(1, 0) + d(0, -1) + d(0, 1))
+           + scal(quarter, d(-1, -1) + d(1, -1) + d(-1, 1) + d(1, 1));
+  };
+  if (ci > 0 && cj > 0 && ci < nc - 1 && cj < nc - 1) body(NAccI<S, R>{xb, nf, m}, NAccI<S, R>{bb, nf, m});
+  else {
+    const Seam<R> seam = seam_load<R>(ph, K, k, nf);
+    body(NAcc<S, R>{xb, nf, m, seam}, NAcc<S, R>{bb, nf, m, seam});
+  }
+  Store<S, R>::st(c + Lc.node(k, cj, ci, v), sres);
+}
+
 constexpr int RR_CH = 8;
 template <typename S, typename R>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_node_residual_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc diag, Sc off,
@@ -1405,12 +1445,31 @@ static int L_node_gs_rows(int n, int m, int K, const double* ph, double alpha, i
   else
     return L_node_gs_rows_d<S, R, 18, 3>(n, m, K, ph, alpha, j0, jstep, nrows, backward, b, x, st);
 }
+// The strips pay from 2^25 (coarse node, vector, k-point) triples on
+// (the default of g_rr_strips): measured at 32 k-points and 16 vectors,
+// 0.757 against 0.813 ms for 256^2 coarse nodes, 0.266 against 0.236 ms for
+// 128^2 and several times slower below (a thread's strip is a dependent
+// chain; small batches leave too few of them).
+static int g_rr_strips = 25;
+extern "C" int mxk_node_rr_set_strips(int log2) {
+  if (log2 < 0 || log2 > 62) return (int) cudaErrorInvalidValue;
+  g_rr_strips = log2;
+  return 0;
+}
+extern "C" int mxk_node_rr_get_strips(void) { return g_rr_strips; }
+
 template <typename S, typename R>
 static int L_node_residual_restrict(int nc, int m, int K, const double* ph, double alpha, const void* x,
                                    const void* b, void* c, cudaStream_t st) {
-  const size_t strips = (size_t) nc * ((nc + RR_CH - 1) / RR_CH);
-  k_node_residual_restrict<S, R><<<grd2(strips, m, K), blk2(m), 0, st>>>(
-      nc, m, K, ph, make_sc(alpha * 8.0 / 3.0), make_sc(-alpha / 3.0), (const S*) x, (const S*) b, (S*) c);
+  const Sc diag = make_sc(alpha * 8.0 / 3.0), off = make_sc(-alpha / 3.0);
+  if ((size_t) nc * nc * m * K >= ((size_t) 1 << g_rr_strips)) {
+    const size_t strips = (size_t) nc * ((nc + RR_CH - 1) / RR_CH);
+    k_node_residual_restrict<S, R><<<grd2(strips, m, K), blk2(m), 0, st>>>(nc, m, K, ph, diag, off, (const S*) x,
+                                                                         (const S*) b, (S*) c);
+  } else {
+    k_node_residual_restrict_site<S, R><<<grd2((size_t) nc * nc, m, K), blk2(m), 0, st>>>(
+        nc, m, K, ph, diag, off, (const S*) x, (const S*) b, (S*) c);
+  }
   MX_CHECK_LAUNCH();
   return 0;
 }

@@ -129,11 +129,14 @@ def test_tuning_get_set_without_gpu(built):
     out-of-range shapes are refused, the autotuner needs a device."""
     import maxwell_gb300 as mx
     t0 = mx.get_tuning()
-    assert t0 == {"gram_waves": 4, "combine_ctas": 2, "residual_sites": 32, "node_strip": 0, "node_band": 16}
-    mx.set_tuning(8, 1, 64, 64, 8)
-    want = {"gram_waves": 8, "combine_ctas": 1, "residual_sites": 64, "node_strip": 64, "node_band": 8}
+    assert t0 == {"gram_waves": 4, "combine_ctas": 2, "residual_sites": 32, "node_strip": 0, "node_band": 16,
+                  "restrict_strip_log2": 25}
+    mx.set_tuning(8, 1, 64, 64, 8, 0)
+    want = {"gram_waves": 8, "combine_ctas": 1, "residual_sites": 64, "node_strip": 64, "node_band": 8,
+            "restrict_strip_log2": 0}
     assert mx.get_tuning() == want
-    for bad in ((0, 2, 32), (4, 17, 32), (4, 2, 0), (65, 2, 32), (4, 2, 32, 96, 8), (4, 2, 32, 64, 0)):
+    for bad in ((0, 2, 32), (4, 17, 32), (4, 2, 0), (65, 2, 32), (4, 2, 32, 96, 8), (4, 2, 32, 64, 0),
+                (4, 2, 32, 0, 16, -1), (4, 2, 32, 0, 16, 63)):
         with pytest.raises(RuntimeError):
             mx.set_tuning(*bad)
     assert mx.get_tuning() == want

@@ -27,11 +27,13 @@ def test_autotune_choice_and_solve(golden):
         assert t["combine_ctas"] in (1, 2, 3, 4)
         assert t["residual_sites"] in (8, 16, 32, 64, 128)
         assert t["node_strip"] in (0, 64, 128) and t["node_band"] in (4, 8, 16, 32, 64)
+        assert t["restrict_strip_log2"] == default["restrict_strip_log2"]   # not searched
         assert mx.get_tuning() == t
-        # the extreme shapes too
-        for shape in ({"gram_waves": 1, "combine_ctas": 1, "residual_sites": 128, "node_strip": 64, "node_band": 1},
+        # the extreme shapes too (strips of coarse rows at every level, and at none)
+        for shape in ({"gram_waves": 1, "combine_ctas": 1, "residual_sites": 128, "node_strip": 64, "node_band": 1,
+                       "restrict_strip_log2": 0},
                       {"gram_waves": 16, "combine_ctas": 4, "residual_sites": 8, "node_strip": 128,
-                       "node_band": 64}, t):
+                       "node_band": 64, "restrict_strip_log2": 62}, t):
             mx.set_tuning(**shape)
             lam, res = _solve(g)
             want = g["lam"][:, :int(g["ieigs"])]

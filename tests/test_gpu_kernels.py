@@ -178,10 +178,12 @@ def test_solver_smoothers_agree(oracle, smoother):
 
 @pytest.mark.parametrize("n", [44, 64])
 @pytest.mark.parametrize("prec", [mx.C128, mx.CDD, mx.C64])
-def test_residual_restriction_strips(oracle, n, prec):
-    """The fused node residual + restriction walks strips of 8 coarse rows:
-    coarse grids of 22 and 32 rows hold strips inside the cell (no seam
-    test), strips along the seam and a ragged last strip."""
+@pytest.mark.parametrize("strips", [True, False])
+def test_residual_restriction_strips(oracle, n, prec, strips):
+    """The fused node residual + restriction in both forms: a thread per
+    coarse node, and (forced here by restrict_strip_log2 = 0) strips of 8
+    coarse rows -- coarse grids of 22 and 32 rows hold strips inside the
+    cell (no seam test), strips along the seam and a ragged last strip."""
     rng = np.random.default_rng(n)
     K, m, nc = 3, 3, n // 2
     kap = 1.0 / (1.0 + 11.0 * rng.random(n * n))
@@ -189,7 +191,12 @@ def test_residual_restriction_strips(oracle, n, prec):
     gc = gf.coarsen()
     x, b, c = cv(rng, K, m, n * n), cv(rng, K, m, n * n), cv(rng, K, m, nc * nc)
     nx, nb, nco = mx.Node(gf, m, prec, x), mx.Node(gf, m, prec, b), mx.Node(gc, m, prec, c)
-    mx.check(mx.lib().residual_restriction_node2d_gpu(mx.fz(0.8), nb.h, nx.h, nco.h))
+    default = mx.get_tuning()
+    try:
+        mx.set_tuning(**dict(default, restrict_strip_log2=0 if strips else 62))
+        mx.check(mx.lib().residual_restriction_node2d_gpu(mx.fz(0.8), nb.h, nx.h, nco.h))
+    finally:
+        mx.set_tuning(**default)
     want = np.array([[oracle.restrict_node(nc, *FACTORS[k], 1.0,
                                            oracle.addeval_node(n, *FACTORS[k], -0.8, x[k, i], b[k, i]),
                                            np.zeros(nc * nc)) for i in range(m)] for k in range(K)])
