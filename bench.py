@@ -354,7 +354,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "clocks": clock,
-        "roofline": roof("node_gs", "k_node_gs_warp + k_node_gs_row (node Gauss-Seidel of the gradient "
+        "roofline": roof("node_gs", "k_node_gs_warp + k_node_gs_rowpar (node Gauss-Seidel of the gradient "
                                     "lifting, finest level)", "one node GS sweep (4 launches)",
                          TRAFFIC_32K["node_gs"]),
         "roofline_more": [roof("gram", "k_block_gram_split + k_gram_reduce (Gram matrices of [E X P])",
