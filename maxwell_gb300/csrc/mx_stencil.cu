@@ -720,10 +720,13 @@ __global__ void k_node_residual_restrict_site(int nc, int m, int K, const double
   Store<S, R>::st(c + Lc.node(k, cj, ci, v), sres);
 }
 
+// coarse rows per strip; the FP32 form is held to 80 registers (3 CTAs per
+// SM, a few spilled values) -- at 124 registers it ran 0.906 against 0.741 ms
 constexpr int RR_CH = 8;
 template <typename S, typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) k_node_residual_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc diag, Sc off,
-                                         const S* __restrict__ x, const S* __restrict__ b, S* __restrict__ c) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1)
+    k_node_residual_restrict(int nc, int m, int K, const double* __restrict__ ph, Sc diag, Sc off,
+                             const S* __restrict__ x, const S* __restrict__ b, S* __restrict__ c) {
   const int nf = 2 * nc, nst = (nc + RR_CH - 1) / RR_CH;
   // block (m, columns): x = vector, y = (column, strip); grid.y = k-point
   const int k = blockIdx.y, v = threadIdx.x;
