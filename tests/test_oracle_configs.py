@@ -42,10 +42,10 @@ def test_oracle_matches_config1_reference(oracle, golden):
     assert (np.abs(lam[:, :ie] - want) / want).max() < 1e-8
 
 
-def test_chern_sums_do_not_depend_on_the_eigenvector_phases(oracle, golden):
-    """The sign continuity absorbs any phase of the input eigenvectors: Chern
-    partial sums along the reference driver's curve are the same when every
-    eigenvector of every point is multiplied by a random unit phase."""
+@pytest.fixture(scope="module")
+def driver_curve(oracle, golden):
+    """The oracle's solve of the reference driver's 16^2 Kivshar curve
+    (Gamma-X-M-Gamma, 4 steps per edge) with its eigenvectors."""
     g = golden("bloch_curve_n16_kivshar.npz")
     n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
     n = n0 << L
@@ -57,9 +57,41 @@ def test_chern_sums_do_not_depend_on_the_eigenvector_phases(oracle, golden):
     assert st == 0
     nk = len(fac)
     vertex = np.array([1 if p in (0, 4, 8, nk - 1) else 0 for p in range(nk)], np.int32)
+    return g, n, fac, ie, m, lam, vec, vertex
+
+
+def test_chern_sums_do_not_depend_on_the_eigenvector_phases(oracle, driver_curve):
+    """The sign continuity absorbs any phase of the input eigenvectors: Chern
+    partial sums along the reference driver's curve are the same when every
+    eigenvector of every point is multiplied by a random unit phase."""
+    g, n, fac, ie, m, lam, vec, vertex = driver_curve
+    nk = len(fac)
     _, _, ch1, _ = oracle.continuity(n, fac, ie, vertex, "s", ie, vec, lam)
     rng = np.random.default_rng(3)
     ph = np.exp(2j * np.pi * rng.random((nk, m)))[:, :, None]
     _, _, ch2, _ = oracle.continuity(n, fac, ie, vertex, "s", ie, vec * ph, lam)
     assert np.abs(ch1 - ch2).max() < 1e-12
     assert np.abs(ch1[1:]).max() > 1e-3       # the sums are not trivially zero
+
+
+def test_chern_increments_match_the_driver_protocol(oracle, driver_curve):
+    """Pin of the continuity restatement against the reference driver's own
+    protocol file (exp_bloch2d.c:1058-1216, 1227-1235; the fixture keeps its
+    6-decimal Chern partial sums).  The sums themselves are anchored on
+    Gamma, where the driver keeps the two constant-field zero modes in an
+    arbitrary basis, so they are compared as increments from point to point,
+    on the stretches where the alignment does not reach back to Gamma: after
+    the vertex X for the bands that stay simple (1st and 4th: the 2nd and
+    3rd meet at M, 12.280956 twice), and on the X-M edge before M for all
+    four.  Tolerance: two 6-decimal roundings."""
+    g, n, fac, ie, m, lam, vec, vertex = driver_curve
+    _, _, ch, _ = oracle.continuity(n, fac, ie, vertex, "s", ie, vec, lam)
+    got, want = np.diff(ch, axis=0), np.diff(g["chern"], axis=0)   # row r: point r -> r + 1
+    x_point, m_point = 4, 8
+    assert np.isclose(g["lam"][m_point, 1], g["lam"][m_point, 2], rtol=1e-6)   # the degeneracy at M
+    simple = [0, 3]
+    d = np.abs(got[x_point:, simple] - want[x_point:, simple]).max()
+    assert d < 3e-6, d
+    d = np.abs(got[x_point:m_point - 1] - want[x_point:m_point - 1]).max()
+    assert d < 3e-6, d
+    assert np.abs(want[x_point:]).max() > 1e-2   # the compared increments are not trivially small
