@@ -78,6 +78,22 @@ def test_surface_matches_oracle(oracle):
     assert np.abs(got - lam_o[:, :ie]).max() / lam_o[:, :ie].max() < 1e-8
 
 
+def test_surface_matches_reference_driver(oracle, golden):
+    """mxg_bloch_surface on the reference surface driver's own full-zone grid
+    (exp_blochsurf: Kivshar disc, 16^2, 4 x 4 k-points, absolute residual
+    1e-8; tests/golden/gen_blochsurf.py): eigenvalues agree with the
+    driver's protocol to its 6 decimals."""
+    g = golden("blochsurf_n16_kivshar.npz")
+    n0, L, ie, m, tol = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"]), float(g["tol"])
+    kap = oracle.disc_kappa(n0 << L, [g["disc"]], float(g["eps_base"]))
+    s = mx.Solver(kap, n0=n0, L=L, ieigs=ie, m=m, method=1, precision=1, wave=8, relative=0, tol=tol,
+                  max_nested=40, max_steps=80)
+    lam, st, res = s.surface(int(g["steps"]))   # [iy, ix]
+    assert res[..., :ie].max() <= tol
+    for (ix, iy), want in zip(g["index"], g["lam"]):
+        assert np.abs(lam[iy, ix, :ie] - want[:ie]).max() < 2e-6, (ix, iy)
+
+
 def test_solver_matches_reference_driver_curve(oracle, golden):
     """The mixed LOBPCG solver on the points of the reference driver's own
     run (exp_bloch2d: Kivshar disc, 16^2, 4 steps per edge of its curve,

@@ -95,3 +95,19 @@ def test_chern_increments_match_the_driver_protocol(oracle, driver_curve):
     d = np.abs(got[x_point:m_point - 1] - want[x_point:m_point - 1]).max()
     assert d < 3e-6, d
     assert np.abs(want[x_point:]).max() > 1e-2   # the compared increments are not trivially small
+
+
+def test_oracle_matches_the_surface_driver(oracle, golden):
+    """The restatement's eigenvalues on the reference surface driver's own
+    full-zone grid (exp_blochsurf: Kivshar disc, 16^2, 4 x 4 k-points with
+    k = 2 pi i / 3 - pi, absolute residual 1e-8; tests/golden/gen_blochsurf.py)
+    agree with the driver's protocol to its 6 decimals.  The grid holds M,
+    where the 2nd and 3rd bands meet, and no Gamma."""
+    g = golden("blochsurf_n16_kivshar.npz")
+    n0, L, ie, m = int(g["n0"]), int(g["L"]), int(g["ieigs"]), int(g["m"])
+    kap = oracle.disc_kappa(n0 << L, [g["disc"]], float(g["eps_base"]))
+    st, lam, steps, res, _ = oracle.bloch_solve(kap, g["factors"], n0=n0, L=L, ieigs=ie, m=m, method=1,
+                                                max_nested=40, max_steps=80, tol=float(g["tol"]), relative=0,
+                                                extrapolation="n", wave=1)
+    assert st == 0 and res[:, :ie].max() <= float(g["tol"])
+    assert np.abs(lam[:, :ie] - g["lam"][:, :ie]).max() < 2e-6
